@@ -1,0 +1,547 @@
+// poe2d_api.cpp -- solver contexts behind the C ABI (include/poe2d.h).
+//
+// A context is one model on one GPU: its coefficient planes and C-PML
+// profiles live in HBM once and are shared by all of its shots.  poe_run
+// advances every shot together; the per-step launch sequence is captured
+// once into a CUDA graph of kGraphSteps steps and replayed (the step number
+// is read from each shot's device counter, so the graph never changes).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/poe2d.h"
+#include "poe2d_internal.h"
+
+using namespace poe;
+
+namespace {
+constexpr int kGraphSteps = 64;
+}
+
+struct ShotHost {
+    float *f = nullptr, *mx = nullptr, *mz = nullptr, *src_tab = nullptr, *trace = nullptr;
+    int2 *rec = nullptr;
+    int nrec = 0;
+    int64_t trace_cap = 0;
+    int64_t src_cap = 0;     // entries computed in src_tab
+    int64_t src_n = 0;       // active entries
+    bool src_complete = false;
+    poe_source src{};
+    int64_t src_off = -1;
+    int src_where = SRC_NONE;
+    int64_t steps = 0;
+};
+
+struct poe_ctx {
+    poe_grid g{};
+    ModelDev m{};
+    bool exact = true, kone = true;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    float *coef = nullptr, *px = nullptr, *pz = nullptr;
+    std::vector<ShotHost> shots;
+    ShotDev *shots_dev = nullptr;
+    int64_t *steps_dev = nullptr;
+    int shots_dev_cap = 0;
+    bool shots_dirty = true;
+    int max_rec = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_kernels = 0;
+    int64_t launches = 0;
+    float *scratch = nullptr;   // 2 words for poe_check_finite
+    std::string err;
+};
+
+namespace {
+
+int fail(poe_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+#define CKL(rc)                                                                           \
+    do {                                                                                  \
+        int r_ = (rc);                                                                    \
+        if (r_ != 0)                                                                      \
+            return fail(ctx, POE_ECUDA, std::string("kernel launch: ") +                  \
+                                            cudaGetErrorString((cudaError_t)r_));         \
+    } while (0)
+
+void free_shot(ShotHost &s)
+{
+    cudaFree(s.f);
+    cudaFree(s.mx);
+    cudaFree(s.mz);
+    cudaFree(s.src_tab);
+    cudaFree(s.trace);
+    cudaFree(s.rec);
+    s = ShotHost{};
+}
+
+void drop_graph(poe_ctx *ctx)
+{
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+}
+
+// strip extents from the profiles: a column carries C-PML memory only where
+// a != 0 in one of its profiles (elsewhere b = 1, a = 0 keeps it zero)
+void strips(const float *prof, int n1, int &lo, int &hi)
+{
+    const float *a = prof + POE_PA * n1, *ah = prof + POE_PA_HALF * n1;
+    lo = 0;
+    hi = n1;
+    for (int i = 0; i < n1 / 2; ++i)
+        if (a[i] != 0.0f || ah[i] != 0.0f) lo = i + 1;
+    for (int i = n1 - 1; i >= n1 / 2; --i)
+        if (a[i] != 0.0f || ah[i] != 0.0f) hi = i;
+    if (lo >= hi) {   // strips meet: store the full axis
+        lo = n1;
+        hi = n1;
+    }
+}
+
+Div24 make_div(float h)
+{
+    Div24 q;
+    const double D = 24.0 * (double)h;
+    q.D = (float)D;
+    q.exact_tie = ((double)q.D == D) ? 1 : 0;
+    q.inv = (float)(1.0 / D);
+    return q;
+}
+
+int sync_shots(poe_ctx *ctx)
+{
+    if (!ctx->shots_dirty) return POE_OK;
+    const int ns = (int)ctx->shots.size();
+    if (ns > ctx->shots_dev_cap) {
+        cudaFree(ctx->shots_dev);
+        cudaFree(ctx->steps_dev);
+        ctx->shots_dev = nullptr;
+        ctx->steps_dev = nullptr;
+        const int cap = std::max(ns, 2 * ctx->shots_dev_cap);
+        CK(cudaMalloc(&ctx->shots_dev, sizeof(ShotDev) * cap));
+        CK(cudaMalloc(&ctx->steps_dev, sizeof(int64_t) * cap));
+        ctx->shots_dev_cap = cap;
+    }
+    std::vector<ShotDev> sd(ns);
+    std::vector<int64_t> st(ns);
+    ctx->max_rec = 0;
+    for (int i = 0; i < ns; ++i) {
+        const ShotHost &s = ctx->shots[i];
+        ShotDev &d = sd[i];
+        d.f = s.f;
+        d.mx = s.mx;
+        d.mz = s.mz;
+        d.step = ctx->steps_dev + i;
+        d.src_off = s.src_off;
+        d.src_where = s.src_where;
+        d.src_n = s.src_n;
+        d.src_tab = s.src_tab;
+        d.rec = s.rec;
+        d.nrec = s.nrec;
+        d.trace = s.trace;
+        d.trace_cap = s.trace_cap;
+        st[i] = s.steps;
+        ctx->max_rec = std::max(ctx->max_rec, s.nrec);
+    }
+    if (ns) {
+        CK(cudaMemcpyAsync(ctx->shots_dev, sd.data(), sizeof(ShotDev) * ns, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->steps_dev, st.data(), sizeof(int64_t) * ns, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));   // host vectors go out of scope
+    }
+    drop_graph(ctx);
+    ctx->shots_dirty = false;
+    return POE_OK;
+}
+
+// make the source table of shot s cover steps up to need (1-based)
+int ensure_source(poe_ctx *ctx, ShotHost &s, int64_t need)
+{
+    if (s.src_where == SRC_NONE || s.src_complete || s.src_cap >= need) return POE_OK;
+    int64_t cap = std::max<int64_t>(need, std::max<int64_t>(1024, 2 * s.src_cap));
+    std::vector<float> tab((size_t)cap);
+    int64_t nact = 0;
+    int rc = poe_source_table(&ctx->g, &s.src, cap, tab.data(), &nact);
+    if (rc != POE_OK) return fail(ctx, rc, "source table");
+    cudaFree(s.src_tab);
+    s.src_tab = nullptr;
+    if (nact > 0) {
+        CK(cudaMalloc(&s.src_tab, sizeof(float) * nact));
+        CK(cudaMemcpyAsync(s.src_tab, tab.data(), sizeof(float) * nact, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    s.src_n = nact;
+    s.src_cap = cap;
+    s.src_complete = nact < cap;
+    ctx->shots_dirty = true;
+    return POE_OK;
+}
+
+int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
+{
+    if (s.nrec == 0 || s.trace_cap >= need) return POE_OK;
+    const int64_t cap = std::max<int64_t>(need, std::max<int64_t>(256, s.trace_cap + s.trace_cap / 2));
+    float *nt = nullptr;
+    CK(cudaMalloc(&nt, sizeof(float) * cap * s.nrec));
+    CK(cudaMemsetAsync(nt, 0, sizeof(float) * cap * s.nrec, ctx->stream));
+    if (s.trace && s.trace_cap)
+        CK(cudaMemcpyAsync(nt, s.trace, sizeof(float) * s.trace_cap * s.nrec, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(s.trace);
+    s.trace = nt;
+    s.trace_cap = cap;
+    ctx->shots_dirty = true;
+    return POE_OK;
+}
+
+int kernels_per_step(const poe_ctx *ctx) { return ctx->max_rec > 0 ? 3 : 2; }
+
+int run_direct(poe_ctx *ctx, int64_t nsteps)
+{
+    const int ns = (int)ctx->shots.size();
+    for (int64_t k = 0; k < nsteps; ++k) {
+        CKL(launch_step(ctx->m, ctx->shots_dev, ns, ctx->max_rec, (int)k, ctx->exact, ctx->kone, ctx->stream));
+        ctx->launches += kernels_per_step(ctx);
+    }
+    CKL(launch_advance(ctx->steps_dev, ns, nsteps, ctx->stream));
+    ctx->launches += 1;
+    return POE_OK;
+}
+
+int build_graph(poe_ctx *ctx)
+{
+    const int ns = (int)ctx->shots.size();
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < kGraphSteps && rc == 0; ++k)
+        rc = launch_step(ctx->m, ctx->shots_dev, ns, ctx->max_rec, k, ctx->exact, ctx->kone, ctx->stream);
+    if (rc == 0) rc = launch_advance(ctx->steps_dev, ns, kGraphSteps, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc != 0 || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(ctx, POE_ECUDA, std::string("graph capture: ") +
+                                        cudaGetErrorString(rc ? (cudaError_t)rc : e));
+    }
+    e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        ctx->graph = nullptr;
+        return fail(ctx, POE_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    ctx->graph_kernels = kGraphSteps * kernels_per_step(ctx) + 1;
+    return POE_OK;
+}
+
+ShotHost *get_shot(poe_ctx *ctx, int32_t shot)
+{
+    if (!ctx || shot < 0 || shot >= (int32_t)ctx->shots.size()) return nullptr;
+    return &ctx->shots[shot];
+}
+
+}  // namespace
+
+extern "C" {
+
+int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, const float *prof_z,
+               void *stream, uint32_t flags, poe_ctx **out)
+{
+    if (!out) return POE_EINVAL;
+    *out = nullptr;
+    if (!grid || !coef || !prof_x || !prof_z || grid->NX < 4 || grid->NZ < 4 || !(grid->dx > 0.0f) ||
+        !(grid->dz > 0.0f) || !(grid->dt > 0.0f))
+        return POE_EINVAL;
+    poe_ctx *ctx = new poe_ctx();
+    ctx->g = *grid;
+    ctx->exact = !(flags & POE_CTX_FAST_STENCIL);
+    cudaGetDevice(&ctx->device);
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete ctx;
+            return POE_ECUDA;
+        }
+        ctx->own_stream = true;
+    }
+    const int nx = grid->NX + 1, nz = grid->NZ + 1;
+    ModelDev &m = ctx->m;
+    m.NX = grid->NX;
+    m.NZ = grid->NZ;
+    m.P = ((nx + XH + 4) + 31) / 32 * 32;
+    m.R = nz + 2 * ZH;
+    m.plane = (int64_t)m.P * m.R;
+    m.dt = grid->dt;
+    m.qx = make_div(grid->dx);
+    m.qz = make_div(grid->dz);
+    strips(prof_x, nx, m.xL, m.xR);
+    strips(prof_z, nz, m.zT, m.zB);
+    m.Wx = m.xL + (nx - m.xR);
+    m.Hz = m.zT + (nz - m.zB);
+    // K == 1 everywhere (K_max = 1, cu:843) lets the kernels skip value / K
+    ctx->kone = true;
+    for (int r : {POE_PK, POE_PK_HALF}) {
+        for (int i = 0; i < nx; ++i) ctx->kone &= prof_x[r * nx + i] == 1.0f;
+        for (int i = 0; i < nz; ++i) ctx->kone &= prof_z[r * nz + i] == 1.0f;
+    }
+    auto up_planes = [&](float **dst, const float *src, int nplanes) -> int {
+        CK(cudaMalloc(dst, sizeof(float) * m.plane * nplanes));
+        CK(cudaMemsetAsync(*dst, 0, sizeof(float) * m.plane * nplanes, ctx->stream));
+        for (int p = 0; p < nplanes; ++p)
+            CK(cudaMemcpy2DAsync(*dst + p * m.plane + (int64_t)ZH * m.P + XH, sizeof(float) * m.P,
+                                 src + (int64_t)p * nx * nz, sizeof(float) * nx, sizeof(float) * nx, nz,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+        return POE_OK;
+    };
+    int rc = up_planes(&ctx->coef, coef, POE_NCOEF);
+    if (rc == POE_OK) {
+        std::vector<float> hx((size_t)6 * m.P, 0.0f), hz((size_t)6 * m.R, 0.0f);
+        for (int r = 0; r < 6; ++r) {
+            // outside the grid: b = 1, K = 1, a = 0 (no memory update, no scaling)
+            for (int i = 0; i < m.P; ++i) hx[(size_t)r * m.P + i] = (r == POE_PB || r == POE_PB_HALF || r == POE_PK || r == POE_PK_HALF) ? 1.0f : 0.0f;
+            for (int i = 0; i < m.R; ++i) hz[(size_t)r * m.R + i] = (r == POE_PB || r == POE_PB_HALF || r == POE_PK || r == POE_PK_HALF) ? 1.0f : 0.0f;
+            for (int i = 0; i < nx; ++i) hx[(size_t)r * m.P + XH + i] = prof_x[(size_t)r * nx + i];
+            for (int i = 0; i < nz; ++i) hz[(size_t)r * m.R + ZH + i] = prof_z[(size_t)r * nz + i];
+        }
+        cudaError_t e = cudaMalloc(&ctx->px, sizeof(float) * hx.size());
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->pz, sizeof(float) * hz.size());
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->scratch, sizeof(float) * 4);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->px, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->pz, hz.data(), sizeof(float) * hz.size(), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("upload: ") + cudaGetErrorString(e));
+    }
+    if (rc != POE_OK) {
+        poe_destroy(ctx);
+        return rc;
+    }
+    m.coef = ctx->coef;
+    m.px = ctx->px;
+    m.pz = ctx->pz;
+    *out = ctx;
+    return POE_OK;
+}
+
+int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, int32_t nrec, int32_t *shot_id)
+{
+    if (!ctx) return POE_EINVAL;
+    if (nrec < 0 || (nrec > 0 && !rec)) return fail(ctx, POE_EINVAL, "receivers");
+    const int NX = ctx->g.NX, NZ = ctx->g.NZ;
+    ShotHost s;
+    const ModelDev &m = ctx->m;
+    if (src) {
+        if (src->ix < 0 || src->ix > NX || src->iz < 0 || src->iz > NZ)
+            return fail(ctx, POE_EINVAL, "source outside the grid");
+        if (src->kind != POE_SRC_REF_DGAUSS_P && src->kind != POE_SRC_RICKER_FZ)
+            return fail(ctx, POE_EINVAL, "source kind");
+        if (!(src->f0 > 0.0f)) return fail(ctx, POE_EINVAL, "source f0");
+        s.src = *src;
+        s.src_where = src->kind == POE_SRC_REF_DGAUSS_P ? SRC_P : SRC_FZ;
+        s.src_off = (int64_t)(src->iz + ZH) * m.P + (src->ix + XH);
+    }
+    std::vector<int2> hr((size_t)nrec);
+    for (int i = 0; i < nrec; ++i) {
+        const poe_receiver &r = rec[i];
+        if (r.comp == POE_REC_NONE) {
+            hr[i] = make_int2(0, -1);
+            continue;
+        }
+        if (r.comp < 0 || r.comp > 2 || r.ix < 0 || r.ix > NX || r.iz < 0 || r.iz > NZ)
+            return fail(ctx, POE_EINVAL, "receiver " + std::to_string(i) + " outside the grid");
+        hr[i] = make_int2((int)((int64_t)(r.iz + ZH) * m.P + (r.ix + XH)), r.comp);
+    }
+    if ((int64_t)(NZ + 1 + 2 * ZH) * m.P >= ((int64_t)1 << 31))
+        return fail(ctx, POE_EINVAL, "grid too large for 32-bit receiver offsets");
+    auto bad = [&](cudaError_t e, const char *what) {
+        free_shot(s);
+        return fail(ctx, e == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    const size_t fbytes = sizeof(float) * m.plane * NSTATE;
+    const size_t xbytes = sizeof(float) * 6 * (size_t)(NZ + 1) * m.Wx;
+    const size_t zbytes = sizeof(float) * 6 * (size_t)m.Hz * m.P;
+    if ((e = cudaMalloc(&s.f, fbytes)) != cudaSuccess) return bad(e, "state");
+    if ((e = cudaMemsetAsync(s.f, 0, fbytes, ctx->stream)) != cudaSuccess) return bad(e, "state");
+    if (xbytes) {
+        if ((e = cudaMalloc(&s.mx, xbytes)) != cudaSuccess) return bad(e, "x strips");
+        if ((e = cudaMemsetAsync(s.mx, 0, xbytes, ctx->stream)) != cudaSuccess) return bad(e, "x strips");
+    }
+    if (zbytes) {
+        if ((e = cudaMalloc(&s.mz, zbytes)) != cudaSuccess) return bad(e, "z strips");
+        if ((e = cudaMemsetAsync(s.mz, 0, zbytes, ctx->stream)) != cudaSuccess) return bad(e, "z strips");
+    }
+    if (nrec > 0) {
+        if ((e = cudaMalloc(&s.rec, sizeof(int2) * nrec)) != cudaSuccess) return bad(e, "receivers");
+        if ((e = cudaMemcpyAsync(s.rec, hr.data(), sizeof(int2) * nrec, cudaMemcpyHostToDevice, ctx->stream)) !=
+            cudaSuccess)
+            return bad(e, "receivers");
+    }
+    s.nrec = nrec;
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bad(e, "add shot");
+    ctx->shots.push_back(s);
+    ctx->shots_dirty = true;
+    if (shot_id) *shot_id = (int32_t)ctx->shots.size() - 1;
+    return POE_OK;
+}
+
+int poe_run(poe_ctx *ctx, int64_t nsteps)
+{
+    if (!ctx) return POE_EINVAL;
+    if (nsteps < 0) return fail(ctx, POE_EINVAL, "nsteps < 0");
+    if (ctx->shots.empty()) return fail(ctx, POE_ESTATE, "no shots");
+    if (nsteps == 0) return POE_OK;
+    CK(cudaSetDevice(ctx->device));
+    int rc;
+    for (ShotHost &s : ctx->shots) {
+        if ((rc = ensure_trace(ctx, s, s.steps + nsteps)) != POE_OK) return rc;
+        if ((rc = ensure_source(ctx, s, s.steps + nsteps)) != POE_OK) return rc;
+    }
+    if ((rc = sync_shots(ctx)) != POE_OK) return rc;
+    int64_t left = nsteps;
+    if (left >= kGraphSteps) {
+        if (!ctx->graph && (rc = build_graph(ctx)) != POE_OK) return rc;
+        for (; left >= kGraphSteps; left -= kGraphSteps) {
+            CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+            ctx->launches += ctx->graph_kernels;
+        }
+    }
+    if (left > 0 && (rc = run_direct(ctx, left)) != POE_OK) return rc;
+    for (ShotHost &s : ctx->shots) s.steps += nsteps;
+    return POE_OK;
+}
+
+int poe_sync(poe_ctx *ctx)
+{
+    if (!ctx) return POE_EINVAL;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return POE_OK;
+}
+
+int poe_get_traces(poe_ctx *ctx, int32_t shot, float *host_out, int64_t capacity_floats)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    const int64_t n = s->steps * s->nrec;
+    if (n == 0) return POE_OK;
+    if (!host_out || capacity_floats < n) return fail(ctx, POE_EINVAL, "trace buffer too small");
+    CK(cudaMemcpyAsync(host_out, s->trace, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return POE_OK;
+}
+
+int poe_get_field(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    if (field < 0 || field >= POE_NFIELDS || !host_out) return fail(ctx, POE_EINVAL, "field id");
+    const ModelDev &m = ctx->m;
+    const int nx = m.NX + 1, nz = m.NZ + 1;
+    CK(cudaMemcpy2DAsync(host_out, sizeof(float) * nx, s->f + field * m.plane + (int64_t)ZH * m.P + XH,
+                         sizeof(float) * m.P, sizeof(float) * nx, nz, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return POE_OK;
+}
+
+int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    if (field < 0 || field >= POE_NFIELDS || !host_in) return fail(ctx, POE_EINVAL, "field id");
+    const ModelDev &m = ctx->m;
+    const int nx = m.NX + 1, nz = m.NZ + 1;
+    CK(cudaMemcpy2DAsync(s->f + field * m.plane + (int64_t)ZH * m.P + XH, sizeof(float) * m.P, host_in,
+                         sizeof(float) * nx, sizeof(float) * nx, nz, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return POE_OK;
+}
+
+int poe_steps_done(poe_ctx *ctx, int32_t shot, int64_t *steps)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s || !steps) return fail(ctx, POE_EINVAL, "shot id");
+    *steps = s->steps;
+    return POE_OK;
+}
+
+int poe_reset_shot(poe_ctx *ctx, int32_t shot)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    const ModelDev &m = ctx->m;
+    CK(cudaMemsetAsync(s->f, 0, sizeof(float) * m.plane * NSTATE, ctx->stream));
+    if (s->mx) CK(cudaMemsetAsync(s->mx, 0, sizeof(float) * 6 * (size_t)(m.NZ + 1) * m.Wx, ctx->stream));
+    if (s->mz) CK(cudaMemsetAsync(s->mz, 0, sizeof(float) * 6 * (size_t)m.Hz * m.P, ctx->stream));
+    if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(float) * s->trace_cap * s->nrec, ctx->stream));
+    s->steps = 0;
+    ctx->shots_dirty = true;
+    return sync_shots(ctx);
+}
+
+int poe_check_finite(poe_ctx *ctx, int32_t shot, float threshold, float *max_abs_out)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    const ModelDev &m = ctx->m;
+    std::vector<float> h((size_t)m.plane * 8);
+    CK(cudaMemcpyAsync(h.data(), s->f, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float mx = 0.0f;
+    bool bad = false;
+    for (float v : h) {
+        if (!std::isfinite(v)) bad = true;
+        else mx = std::max(mx, std::fabs(v));
+    }
+    if (max_abs_out) *max_abs_out = bad ? INFINITY : mx;
+    if (bad || (threshold > 0.0f && mx > threshold))
+        return fail(ctx, POE_ENONFINITE, "field not finite or above threshold");
+    return POE_OK;
+}
+
+int poe_kernel_launches(const poe_ctx *ctx, int64_t *count)
+{
+    if (!ctx || !count) return POE_EINVAL;
+    *count = ctx->launches;
+    return POE_OK;
+}
+
+const char *poe_last_error(const poe_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void poe_destroy(poe_ctx *ctx)
+{
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    for (ShotHost &s : ctx->shots) free_shot(s);
+    cudaFree(ctx->shots_dev);
+    cudaFree(ctx->steps_dev);
+    cudaFree(ctx->coef);
+    cudaFree(ctx->px);
+    cudaFree(ctx->pz);
+    cudaFree(ctx->scratch);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+}  // extern "C"
