@@ -1,0 +1,346 @@
+"""Benchmark: the 2-D poroelastic C-PML time loop on GB300.
+
+Workload (one bench step = one complete shot):
+  2001 x 2001 patchy-saturation model, h = 0.5 m, 40-cell C-PML on all sides;
+  sandstone frame (rho_s 2650, phi 0.2, K_s 37 GPa, K_frame 10 GPa,
+  mu 8 GPa, kappa 1e-12, tortuosity 2), water background (K_f 2.25 GPa,
+  rho_f 1000, eta 1e-3) with seeded random circular gas patches (K_gas
+  0.02 GPa, rho_gas 100, eta 1e-5, radii U[2, 10] m, 10 % areal fraction);
+  dt = 5e-5 s, 20000 steps; Ricker f0 = 200 Hz vertical force at the surface
+  centre; 400 surface receivers recording vx, vz and p.
+Inputs are synthetic (seeded), the reference ships no model files.
+
+value: Gcell-updates/s with the model resident in HBM (state reset + 20000
+steps per bench step, CUDA events around K steps).  e2e: the same through
+the C ABI from pinned host buffers: create context (coefficients H2D), run,
+read the traces back (D2H), destroy.  cpu_baseline / --impl reference: the
+CPU oracle (a C restatement of the reference loop, OpenMP over all host
+threads) on a bounded sample of steps of the same model.
+
+Multi-GPU: shots are independent, so N ranks run N replicas (one shot each,
+sources shifted), with no collective on the data path ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched Gcell-updates/s vs 1-shot at 1e-5; surrogate gathers/s at ≤5% L2 err"
+NX = NZ = 2000
+DX, DT, F0, NPML, NSTEPS, NREC = 0.5, 5e-5, 200.0, 40, 20000, 400
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(seed=0, shift=0):
+    import poe2d_gb300 as P
+    from poe2d_gb300.patchy import random_patches
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = P.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    gas = P.biot_material(rho_f=100.0, k_f=0.02e9, eta=1e-5, **frame)
+    ids = random_patches((NZ + 1, NX + 1), DX, fraction=0.10, r_min=2.0, r_max=10.0, seed=1234 + seed)
+    coef, vp = P.coeffs_biot([water, gas], ids)
+    g = P.grid(NX, NZ, DX, DT)
+    P.check_courant(g, vp)
+    px, pz = P.pml_profiles(g, NPML, F0, vp)
+    isrc = (NX + 1) // 2 + shift
+    src = P.source(isrc, NPML, P.SRC_RICKER_FZ, F0, 1e6, 0.0)
+    xs = NPML + 1 + (np.arange(NREC) * (NX - 2 * NPML - 2)) // (NREC - 1)
+    rec = [(int(x), NPML, c) for c in (P.REC_VX, P.REC_VZ, P.REC_P) for x in xs]
+    return g, coef, px, pz, src, rec, ids
+
+
+def alg_bytes_per_step(g, s_ctx_strips):
+    """96 B per cell (8 state fields read+written, 8 coefficients read) plus
+    8 B per C-PML memory variable on its strip (6 x-strip, 6 z-strip)."""
+    nx, nz = g.NX + 1, g.NZ + 1
+    wx, hz = s_ctx_strips
+    return 96 * nx * nz + 48 * nz * wx + 48 * nx * hz
+
+
+def strip_extent(px, pz):
+    def ext(prof):
+        n1 = prof.shape[1]
+        a = (prof[0] != 0) | (prof[3] != 0)
+        lo = max([i + 1 for i in range(n1 // 2) if a[i]], default=0)
+        hi = min([i for i in range(n1 // 2, n1) if a[i]], default=n1)
+        return n1 if lo >= hi else lo + (n1 - hi)
+    return ext(px), ext(pz)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax = float(p[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class CpuOracle:
+    """The oracle on the host cores over the bench model (bounded step samples)."""
+
+    def __init__(self, g, coef, px, pz, src_ix, src_iz, threads=None):
+        from oracle import oracle as O
+        O.build()
+        self.th = threads or os.cpu_count() or 1
+        self.o = O.Oracle(O.REFMIXED, g.NX, g.NZ, g.dx, g.dz, g.dt, coef, px, pz, threads=self.th)
+        tab = O.source_table(1, F0, g.dt, NSTEPS, amplitude=1e6, t_cut=0.0, dx=g.dx, dz=g.dz)
+        self.o.set_source(src_ix, src_iz, O.SRC_FZ, tab)
+        self.o.set_receivers([(src_ix, src_iz, 1)])
+        self.cells = (g.NX + 1) * (g.NZ + 1)
+        self.o.run(2)                     # first touch of every page, thread start-up
+        t0 = time.perf_counter()
+        self.o.run(2)
+        self.per_step = (time.perf_counter() - t0) / 2
+
+    def sample(self, seconds):
+        n = int(min(max(2, seconds / max(self.per_step, 1e-6)), 5000))
+        t0 = time.perf_counter()
+        self.o.run(n)
+        el = time.perf_counter() - t0
+        return n, el
+
+
+def cpu_sample(g, coef, px, pz, src_ix, src_iz, target_s=12.0):
+    c = CpuOracle(g, coef, px, pz, src_ix, src_iz)
+    n, el = c.sample(target_s)
+    return {"value": c.cells * n / el / 1e9, "unit": "Gcell-updates/s", "cores": c.th, "kind": "port",
+            "sample": "%d of the %d steps of the 2001x2001 shot (after 4 untimed), %.1f s" % (n, NSTEPS, el)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args, ws, rank):
+    """CPU reference arm: the oracle restatement of the reference loop (the
+    reference's own CPU program cannot be built on this host), all threads."""
+    if rank != 0:
+        return
+    g, coef, px, pz, src, rec, _ = workload()
+    c = CpuOracle(g, coef, px, pz, src.ix, src.iz)
+    for _ in range(args.warmup):
+        c.o.run(1)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, el = c.sample(5.0)
+        tot_n += n
+        tot_t += el
+    value = c.cells * tot_n / tot_t / 1e9
+    sample = ("%d bench steps, each a sample of ~%d of the %d time steps of the 2001x2001 shot, %.1f s total"
+              % (args.steps, tot_n // max(args.steps, 1), NSTEPS, tot_t))
+    line = {"metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * c.cells * NSTEPS / (value * 1e9), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "2001x2001 patchy shot, 40-cell C-PML, 20000 steps, 400 receivers x (vx,vz,p)",
+                       "arm": "CPU oracle (C restatement of the reference loop, bit-exact with the reference's "
+                              "own code where that builds), OpenMP over all host threads; ms_per_step "
+                              "extrapolates the sample to the full 20000-step shot"},
+            "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": c.th, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    import poe2d_gb300 as P
+    from poe2d_gb300 import build as B
+    B.build()
+
+    g, coef, px, pz, src, rec, ids = workload(seed=0, shift=8 * rank)
+    stream = torch.cuda.current_stream()
+    solver = P.Solver(g, coef, px, pz, stream=stream.cuda_stream)
+    solver.add_shot(src, rec)
+    cells = (g.NX + 1) * (g.NZ + 1)
+
+    def shot():
+        solver.reset_shot(0)
+        solver.run(NSTEPS)
+
+    for _ in range(args.warmup):
+        shot()
+    torch.cuda.synchronize()
+    launches0 = solver.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            shot()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if pg:
+        pg.barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = solver.launches - launches0
+    t = torch.tensor([ms], device="cuda")
+    if pg:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    ms_max = float(t.item())
+    total_cells = cells * NSTEPS * args.steps * ws
+    value = total_cells / (ms_max * 1e-3) / 1e9
+
+    # roofline of the time step: algorithmic bytes per step / time per step
+    hbm, peak_kind = peaks()
+    alg = alg_bytes_per_step(g, strip_extent(px, pz))
+    step_s = ms * 1e-3 / (args.steps * NSTEPS)
+    achieved = alg / step_s / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            tr = json.load(f)
+        traffic = float(tr["dram_bytes_per_cell_update"]) * cells
+    except Exception:
+        pass
+    trace = solver.traces()
+    ok = bool(np.isfinite(trace).all() and np.abs(trace).max() > 0)
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hcoef = torch.empty(coef.shape, dtype=torch.float32, pin_memory=True).numpy()
+        hcoef[...] = coef
+        htr = torch.empty((NSTEPS, len(rec)), dtype=torch.float32, pin_memory=True).numpy()
+        solver.close()
+        e2e_steps = max(1, args.steps)
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s2 = P.Solver(g, hcoef, px, pz, stream=stream.cuda_stream)
+            s2.add_shot(src, rec)
+            s2.run(NSTEPS)
+            P._lib.check(P.lib().poe_get_traces(s2.h, 0, htr.ctypes.data_as(P.solver._fp), htr.size), s2.h)
+            s2.close()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        te = torch.tensor([el], device="cuda")
+        if pg:
+            pg.all_reduce(te, op=pg.ReduceOp.MAX)
+        el = float(te.item())
+        e2e = {"value": cells * NSTEPS * e2e_steps * ws / el / 1e9, "unit": "Gcell-updates/s",
+               "h2d_bytes_per_step": int(coef.nbytes + px.nbytes + pz.nbytes + 12 * len(rec)),
+               "d2h_bytes_per_step": int(htr.nbytes)}
+    else:
+        solver.close()
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_sample(g, coef, px, pz, src.ix, src.iz)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "2001x2001 patchy gas/water sandstone shot, h=0.5 m, 40-cell C-PML, "
+                                   "dt=5e-5 s, 20000 steps, Ricker 200 Hz vertical force, 400 receivers x (vx,vz,p)",
+                       "grid": [g.NX + 1, g.NZ + 1], "time_steps": NSTEPS, "pml": NPML, "receivers": NREC,
+                       "gas_fraction": float(ids.mean()), "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (12 state planes x 16 MB + 8 coefficient planes)",
+                       "stencil_rounding": "exact (FP64 sub-expressions of the reference rounded once)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_step": alg, "step_us": step_s * 1e6},
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "wall_s": wall, "finite": ok,
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

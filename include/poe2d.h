@@ -159,8 +159,10 @@ int poe_source_table(const poe_grid *grid, const poe_source *src, int64_t nsteps
  * block cu:1215-1592).  stream: a cudaStream_t, or NULL for the legacy
  * default stream.  flags: POE_CTX_* below. */
 enum {
-    POE_CTX_FAST_STENCIL = 1 /* plain FP32 stencils instead of rounding them as the reference's
-                                FP64 expressions do (faster, ~1e-6 relative drift) */
+    POE_CTX_FAST_STENCIL = 1, /* plain FP32 stencils instead of rounding them as the reference's
+                                 FP64 expressions do (faster, ~1e-6 relative drift) */
+    POE_CTX_NO_PALETTE = 2    /* keep the 8 coefficient planes even when the model has few
+                                 distinct materials (default: a 1-byte material id per cell) */
 };
 int poe_create(const poe_grid *grid, const float *coef, const float *prof_x,
                const float *prof_z, void *stream, uint32_t flags, poe_ctx **out);

@@ -16,6 +16,7 @@ POE_OK, POE_EINVAL, POE_ECFL, POE_ENONFINITE, POE_ETIMEOUT, POE_ECUDA, POE_ENOME
 SRC_REF_DGAUSS_P, SRC_RICKER_FZ = 0, 1
 REC_NONE, REC_VX, REC_VZ, REC_P = -1, 0, 1, 2
 CTX_FAST_STENCIL = 1
+CTX_NO_PALETTE = 2
 FIELDS = ["vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22", "xi1", "xi2"]
 COEFS = ["rho", "rhof", "rsm", "eok", "lambdac", "mu", "alpha", "rbm"]
 

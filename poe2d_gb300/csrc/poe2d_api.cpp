@@ -5,9 +5,11 @@
 // advances every shot together; the per-step launch sequence is captured
 // once into a CUDA graph of kGraphSteps steps and replayed (the step number
 // is read from each shot's device counter, so the graph never changes).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -24,8 +26,13 @@ constexpr int kGraphSteps = 64;
 }
 
 struct ShotHost {
-    float *f = nullptr, *mx = nullptr, *mz = nullptr, *src_tab = nullptr, *trace = nullptr;
-    int2 *rec = nullptr;
+    float *f[2] = {nullptr, nullptr};       // NSF planes each, one allocation (f[0])
+    CUtensorMap *tm = nullptr;              // device copies: [0] velocity box, [1] state box
+    float *mx[2] = {nullptr, nullptr}, *mz[2] = {nullptr, nullptr};
+    float *mxv = nullptr, *mzv = nullptr, *acc = nullptr;
+    float *src_tab = nullptr, *trace = nullptr;
+    int *rec_start = nullptr;
+    int4 *rec_sorted = nullptr;
     int nrec = 0;
     int64_t trace_cap = 0;
     int64_t src_cap = 0;     // entries computed in src_tab
@@ -46,7 +53,7 @@ struct poe_ctx {
     int device = 0;
     float *coef = nullptr, *px = nullptr, *pz = nullptr;
     std::vector<ShotHost> shots;
-    ShotDev *shots_dev = nullptr;
+    StreamShot *shots_dev = nullptr;
     int64_t *steps_dev = nullptr;
     int shots_dev_cap = 0;
     bool shots_dirty = true;
@@ -54,7 +61,13 @@ struct poe_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_kernels = 0;
     int64_t launches = 0;
-    float *scratch = nullptr;   // 2 words for poe_check_finite
+    float *derived = nullptr;   // 3 planes: sigma_xx, sigma_zz, p on demand
+    int *err_dev = nullptr;     // set by a kernel whose bounded wait gave up
+    uint8_t *ids = nullptr;     // palette mode: material id plane
+    float *mtab = nullptr;      // palette mode: material table
+    CUtensorMap *tm_ids = nullptr;
+    int nmat = 0;
+    int ntx = 1, ntz = 1;       // tiles across x and z
     std::string err;
 };
 
@@ -84,12 +97,19 @@ int fail(poe_ctx *c, int code, const std::string &msg)
 
 void free_shot(ShotHost &s)
 {
-    cudaFree(s.f);
-    cudaFree(s.mx);
-    cudaFree(s.mz);
+    cudaFree(s.f[0]);
+    cudaFree(s.tm);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(s.mx[i]);
+        cudaFree(s.mz[i]);
+    }
+    cudaFree(s.mxv);
+    cudaFree(s.mzv);
+    cudaFree(s.acc);
     cudaFree(s.src_tab);
     cudaFree(s.trace);
-    cudaFree(s.rec);
+    cudaFree(s.rec_start);
+    cudaFree(s.rec_sorted);
     s = ShotHost{};
 }
 
@@ -136,33 +156,41 @@ int sync_shots(poe_ctx *ctx)
         ctx->shots_dev = nullptr;
         ctx->steps_dev = nullptr;
         const int cap = std::max(ns, 2 * ctx->shots_dev_cap);
-        CK(cudaMalloc(&ctx->shots_dev, sizeof(ShotDev) * cap));
+        CK(cudaMalloc(&ctx->shots_dev, sizeof(StreamShot) * cap));
         CK(cudaMalloc(&ctx->steps_dev, sizeof(int64_t) * cap));
         ctx->shots_dev_cap = cap;
     }
-    std::vector<ShotDev> sd(ns);
+    std::vector<StreamShot> sd(ns);
     std::vector<int64_t> st(ns);
     ctx->max_rec = 0;
     for (int i = 0; i < ns; ++i) {
         const ShotHost &s = ctx->shots[i];
-        ShotDev &d = sd[i];
-        d.f = s.f;
-        d.mx = s.mx;
-        d.mz = s.mz;
+        StreamShot &d = sd[i];
+        for (int b = 0; b < 2; ++b) {
+            d.f[b] = s.f[b];
+            d.mx[b] = s.mx[b];
+            d.mz[b] = s.mz[b];
+        }
+        d.mxv = s.mxv;
+        d.mzv = s.mzv;
+        d.acc = s.acc;
         d.step = ctx->steps_dev + i;
         d.src_off = s.src_off;
         d.src_where = s.src_where;
         d.src_n = s.src_n;
         d.src_tab = s.src_tab;
-        d.rec = s.rec;
+        d.rec_start = s.rec_start;
+        d.rec_sorted = s.rec_sorted;
         d.nrec = s.nrec;
         d.trace = s.trace;
         d.trace_cap = s.trace_cap;
+        d.tm_v = s.tm ? (const void *)&s.tm[0] : nullptr;
+        d.tm_s = s.tm ? (const void *)&s.tm[1] : nullptr;
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
     }
     if (ns) {
-        CK(cudaMemcpyAsync(ctx->shots_dev, sd.data(), sizeof(ShotDev) * ns, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->shots_dev, sd.data(), sizeof(StreamShot) * ns, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->steps_dev, st.data(), sizeof(int64_t) * ns, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));   // host vectors go out of scope
     }
@@ -212,13 +240,18 @@ int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
     return POE_OK;
 }
 
-int kernels_per_step(const poe_ctx *ctx) { return ctx->max_rec > 0 ? 3 : 2; }
+int kernels_per_step(const poe_ctx *) { return 1; }
+
+int step_launch(poe_ctx *ctx, int k)
+{
+    return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), k, ctx->exact, ctx->kone, ctx->stream);
+}
 
 int run_direct(poe_ctx *ctx, int64_t nsteps)
 {
     const int ns = (int)ctx->shots.size();
     for (int64_t k = 0; k < nsteps; ++k) {
-        CKL(launch_step(ctx->m, ctx->shots_dev, ns, ctx->max_rec, (int)k, ctx->exact, ctx->kone, ctx->stream));
+        CKL(step_launch(ctx, (int)k));
         ctx->launches += kernels_per_step(ctx);
     }
     CKL(launch_advance(ctx->steps_dev, ns, nsteps, ctx->stream));
@@ -233,7 +266,7 @@ int build_graph(poe_ctx *ctx)
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int k = 0; k < kGraphSteps && rc == 0; ++k)
-        rc = launch_step(ctx->m, ctx->shots_dev, ns, ctx->max_rec, k, ctx->exact, ctx->kone, ctx->stream);
+        rc = step_launch(ctx, k);
     if (rc == 0) rc = launch_advance(ctx->steps_dev, ns, kGraphSteps, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -249,6 +282,109 @@ int build_graph(poe_ctx *ctx)
     }
     ctx->graph_kernels = kGraphSteps * kernels_per_step(ctx) + 1;
     return POE_OK;
+}
+
+// after a stream sync: POE_ETIMEOUT if a kernel reported a bounded wait that gave up
+int device_status(poe_ctx *ctx)
+{
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->err_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        CK(cudaMemsetAsync(ctx->err_dev, 0, sizeof(int), ctx->stream));
+        return fail(ctx, POE_ETIMEOUT, "a kernel's bounded wait for its shared-memory copies gave up");
+    }
+    return POE_OK;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// TMA descriptor of a stack of float planes (pitch P, R rows, nplanes) with a
+// (box_w x box_h x 1) box
+bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes, int box_w, int box_h)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)m.P, (cuuint64_t)m.R, (cuuint64_t)nplanes};
+    cuuint64_t strides[2] = {(cuuint64_t)m.P * 4, (cuuint64_t)m.plane * 4};
+    cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool encode_ids(CUtensorMap *out, uint8_t *base, const ModelDev &m)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)m.P, (cuuint64_t)m.R};
+    cuuint64_t strides[1] = {(cuuint64_t)m.P};
+    cuuint32_t box[2] = {(cuuint32_t)TMA_IW, (cuuint32_t)TMA_IH};
+    cuuint32_t es[2] = {1, 1};
+    return fn(out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Palette of the coefficient planes: ids (one byte per cell) and table rows
+// holding the 8 coefficients plus what the reference derives from them per
+// cell, with the reference's float operations (cu:293-295, 311).  False if
+// there are more than MAX_PALETTE distinct cells.
+bool build_palette(const float *coef, int64_t ncell, float dt, std::vector<uint8_t> &ids, std::vector<float> &tab)
+{
+    std::vector<std::array<uint32_t, POE_NCOEF>> keys;
+    ids.resize((size_t)ncell);
+    int last = -1;
+    for (int64_t j = 0; j < ncell; ++j) {
+        std::array<uint32_t, POE_NCOEF> key;
+        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&key[c], coef + c * ncell + j, 4);
+        int id = -1;
+        if (last >= 0 && keys[last] == key) id = last;
+        for (int i = 0; id < 0 && i < (int)keys.size(); ++i)
+            if (keys[i] == key) id = i;
+        if (id < 0) {
+            if ((int)keys.size() >= MAX_PALETTE) return false;
+            keys.push_back(key);
+            id = (int)keys.size() - 1;
+        }
+        ids[(size_t)j] = (uint8_t)id;
+        last = id;
+    }
+    tab.assign(keys.size() * MT_W, 0.0f);
+    for (size_t i = 0; i < keys.size(); ++i) {
+        float *t = tab.data() + i * MT_W;
+        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&t[c], &keys[i][c], 4);
+        const float rho = t[POE_C_RHO], rhof = t[POE_C_RHOF], rsm = t[POE_C_RSM], eok = t[POE_C_EOK];
+        const float co = (rho * rsm - rhof * rhof) / dt;
+        t[MT_RHOF_EOK] = rhof * eok;
+        t[MT_CO] = co;
+        t[MT_C1] = co + rho * eok * 0.5f;
+        t[MT_C2] = co - rho * eok * 0.5f;
+        t[MT_RCO] = (float)(1.0 / (double)co);
+        t[MT_RC1] = (float)(1.0 / (double)t[MT_C1]);
+        if (!std::isfinite(t[MT_RCO]) || !std::isfinite(t[MT_RC1]) || !std::isnormal(co) ||
+            !std::isnormal(t[MT_C1]))
+            return false;   // degenerate material: keep the plane path and IEEE division
+    }
+    return true;
 }
 
 ShotHost *get_shot(poe_ctx *ctx, int32_t shot)
@@ -287,8 +423,11 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     ModelDev &m = ctx->m;
     m.NX = grid->NX;
     m.NZ = grid->NZ;
-    m.P = ((nx + XH + 4) + 31) / 32 * 32;
-    m.R = nz + 2 * ZH;
+    ctx->ntx = (nx + TILE_X - 1) / TILE_X;
+    ctx->ntz = (nz + TILE_Z - 1) / TILE_Z;
+    // tiles read columns x0-4 .. x0+75 (ids) and rows z0-4 .. z0+35 of their halo
+    m.P = (std::max(ctx->ntx * TILE_X + 16, XH + nx + 4) + 31) / 32 * 32;
+    m.R = ctx->ntz * TILE_Z + 8;
     m.plane = (int64_t)m.P * m.R;
     m.dt = grid->dt;
     m.qx = make_div(grid->dx);
@@ -312,19 +451,47 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
                                  cudaMemcpyHostToDevice, ctx->stream));
         return POE_OK;
     };
-    int rc = up_planes(&ctx->coef, coef, POE_NCOEF);
+    int rc = POE_OK;
+    // palette mode when the model has few distinct materials (patchy models)
+    std::vector<uint8_t> hid;
+    std::vector<float> htab;
+    const bool pal = !(flags & POE_CTX_NO_PALETTE) && encode_fn() &&
+                     build_palette(coef, (int64_t)nx * nz, grid->dt, hid, htab);
+    if (pal) {
+        ctx->nmat = (int)(htab.size() / MT_W);
+        cudaError_t e = cudaMalloc(&ctx->ids, (size_t)m.P * m.R);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->ids, 0, (size_t)m.P * m.R, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(ctx->ids + (size_t)ZH * m.P + XH, m.P, hid.data(), nx, nx, nz,
+                                  cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->mtab, sizeof(float) * htab.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->mtab, htab.data(), sizeof(float) * htab.size(), cudaMemcpyHostToDevice,
+                                ctx->stream);
+        CUtensorMap tmi;
+        if (e == cudaSuccess && !encode_ids(&tmi, ctx->ids, m)) e = cudaErrorInvalidValue;
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->tm_ids, sizeof(CUtensorMap));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->tm_ids, &tmi, sizeof(CUtensorMap), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("palette upload: ") + cudaGetErrorString(e));
+    } else {
+        rc = up_planes(&ctx->coef, coef, POE_NCOEF);
+    }
     if (rc == POE_OK) {
         std::vector<float> hx((size_t)6 * m.P, 0.0f), hz((size_t)6 * m.R, 0.0f);
         for (int r = 0; r < 6; ++r) {
             // outside the grid: b = 1, K = 1, a = 0 (no memory update, no scaling)
-            for (int i = 0; i < m.P; ++i) hx[(size_t)r * m.P + i] = (r == POE_PB || r == POE_PB_HALF || r == POE_PK || r == POE_PK_HALF) ? 1.0f : 0.0f;
-            for (int i = 0; i < m.R; ++i) hz[(size_t)r * m.R + i] = (r == POE_PB || r == POE_PB_HALF || r == POE_PK || r == POE_PK_HALF) ? 1.0f : 0.0f;
+            const bool one = r == POE_PB || r == POE_PB_HALF || r == POE_PK || r == POE_PK_HALF;
+            for (int i = 0; i < m.P; ++i) hx[(size_t)r * m.P + i] = one ? 1.0f : 0.0f;
+            for (int i = 0; i < m.R; ++i) hz[(size_t)r * m.R + i] = one ? 1.0f : 0.0f;
             for (int i = 0; i < nx; ++i) hx[(size_t)r * m.P + XH + i] = prof_x[(size_t)r * nx + i];
             for (int i = 0; i < nz; ++i) hz[(size_t)r * m.R + ZH + i] = prof_z[(size_t)r * nz + i];
         }
         cudaError_t e = cudaMalloc(&ctx->px, sizeof(float) * hx.size());
+        if (e == cudaSuccess) e = cudaMalloc(&ctx->err_dev, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->err_dev, 0, sizeof(int), ctx->stream);
         if (e == cudaSuccess) e = cudaMalloc(&ctx->pz, sizeof(float) * hz.size());
-        if (e == cudaSuccess) e = cudaMalloc(&ctx->scratch, sizeof(float) * 4);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ctx->px, hx.data(), sizeof(float) * hx.size(), cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess)
@@ -339,6 +506,11 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     m.coef = ctx->coef;
     m.px = ctx->px;
     m.pz = ctx->pz;
+    m.err = ctx->err_dev;
+    m.ids = ctx->ids;
+    m.mtab = ctx->mtab;
+    m.nmat = ctx->nmat;
+    m.tm_ids = ctx->tm_ids;
     *out = ctx;
     return POE_OK;
 }
@@ -348,8 +520,8 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     if (!ctx) return POE_EINVAL;
     if (nrec < 0 || (nrec > 0 && !rec)) return fail(ctx, POE_EINVAL, "receivers");
     const int NX = ctx->g.NX, NZ = ctx->g.NZ;
-    ShotHost s;
     const ModelDev &m = ctx->m;
+    ShotHost s;
     if (src) {
         if (src->ix < 0 || src->ix > NX || src->iz < 0 || src->iz > NZ)
             return fail(ctx, POE_EINVAL, "source outside the grid");
@@ -360,42 +532,76 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
         s.src_where = src->kind == POE_SRC_REF_DGAUSS_P ? SRC_P : SRC_FZ;
         s.src_off = (int64_t)(src->iz + ZH) * m.P + (src->ix + XH);
     }
-    std::vector<int2> hr((size_t)nrec);
+    // receivers: CSR over tiles, so each tile records its own
+    const int ncell = ctx->ntx * ctx->ntz;
+    std::vector<int> start((size_t)ncell + 1, 0);
+    std::vector<int4> sorted;
     for (int i = 0; i < nrec; ++i) {
         const poe_receiver &r = rec[i];
-        if (r.comp == POE_REC_NONE) {
-            hr[i] = make_int2(0, -1);
-            continue;
-        }
+        if (r.comp == POE_REC_NONE) continue;
         if (r.comp < 0 || r.comp > 2 || r.ix < 0 || r.ix > NX || r.iz < 0 || r.iz > NZ)
             return fail(ctx, POE_EINVAL, "receiver " + std::to_string(i) + " outside the grid");
-        hr[i] = make_int2((int)((int64_t)(r.iz + ZH) * m.P + (r.ix + XH)), r.comp);
+        start[(size_t)(r.iz / TILE_Z) * ctx->ntx + r.ix / TILE_X + 1]++;
     }
-    if ((int64_t)(NZ + 1 + 2 * ZH) * m.P >= ((int64_t)1 << 31))
-        return fail(ctx, POE_EINVAL, "grid too large for 32-bit receiver offsets");
+    for (int c = 0; c < ncell; ++c) start[c + 1] += start[c];
+    sorted.resize((size_t)start[ncell]);
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int i = 0; i < nrec; ++i) {
+            const poe_receiver &r = rec[i];
+            if (r.comp == POE_REC_NONE) continue;
+            sorted[fill[(size_t)(r.iz / TILE_Z) * ctx->ntx + r.ix / TILE_X]++] = make_int4(r.ix, r.comp, i, r.iz);
+        }
+    }
     auto bad = [&](cudaError_t e, const char *what) {
         free_shot(s);
         return fail(ctx, e == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,
                     std::string(what) + ": " + cudaGetErrorString(e));
     };
     cudaError_t e;
-    const size_t fbytes = sizeof(float) * m.plane * NSTATE;
-    const size_t xbytes = sizeof(float) * 6 * (size_t)(NZ + 1) * m.Wx;
-    const size_t zbytes = sizeof(float) * 6 * (size_t)m.Hz * m.P;
-    if ((e = cudaMalloc(&s.f, fbytes)) != cudaSuccess) return bad(e, "state");
-    if ((e = cudaMemsetAsync(s.f, 0, fbytes, ctx->stream)) != cudaSuccess) return bad(e, "state");
+    const size_t fbytes = sizeof(float) * m.plane * NSF;
+    const size_t xbytes = sizeof(float) * 3 * (size_t)(NZ + 1) * m.Wx;
+    const size_t zbytes = sizeof(float) * 3 * (size_t)m.Hz * m.P;
+    if ((e = cudaMalloc(&s.f[0], 2 * fbytes)) != cudaSuccess) return bad(e, "state");
+    if ((e = cudaMemsetAsync(s.f[0], 0, 2 * fbytes, ctx->stream)) != cudaSuccess) return bad(e, "state");
+    s.f[1] = s.f[0] + NSF * m.plane;
+    if (ctx->ids) {
+        CUtensorMap tm[2];
+        if (!encode_planes(&tm[0], s.f[0], m, 2 * NSF, TMA_VW, TMA_VH) ||
+            !encode_planes(&tm[1], s.f[0], m, 2 * NSF, TMA_VW, TMA_SH))
+            return bad(cudaErrorInvalidValue, "TMA descriptor");
+        if ((e = cudaMalloc(&s.tm, sizeof(tm))) != cudaSuccess) return bad(e, "TMA descriptor");
+        if ((e = cudaMemcpyAsync(s.tm, tm, sizeof(tm), cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+            return bad(e, "TMA descriptor");
+    }
+    for (int b = 0; b < 2; ++b) {
+        if (xbytes) {
+            if ((e = cudaMalloc(&s.mx[b], xbytes)) != cudaSuccess) return bad(e, "x strips");
+            if ((e = cudaMemsetAsync(s.mx[b], 0, xbytes, ctx->stream)) != cudaSuccess) return bad(e, "x strips");
+        }
+        if (zbytes) {
+            if ((e = cudaMalloc(&s.mz[b], zbytes)) != cudaSuccess) return bad(e, "z strips");
+            if ((e = cudaMemsetAsync(s.mz[b], 0, zbytes, ctx->stream)) != cudaSuccess) return bad(e, "z strips");
+        }
+    }
     if (xbytes) {
-        if ((e = cudaMalloc(&s.mx, xbytes)) != cudaSuccess) return bad(e, "x strips");
-        if ((e = cudaMemsetAsync(s.mx, 0, xbytes, ctx->stream)) != cudaSuccess) return bad(e, "x strips");
+        if ((e = cudaMalloc(&s.mxv, xbytes)) != cudaSuccess) return bad(e, "x strips");
+        if ((e = cudaMemsetAsync(s.mxv, 0, xbytes, ctx->stream)) != cudaSuccess) return bad(e, "x strips");
     }
     if (zbytes) {
-        if ((e = cudaMalloc(&s.mz, zbytes)) != cudaSuccess) return bad(e, "z strips");
-        if ((e = cudaMemsetAsync(s.mz, 0, zbytes, ctx->stream)) != cudaSuccess) return bad(e, "z strips");
+        if ((e = cudaMalloc(&s.mzv, zbytes)) != cudaSuccess) return bad(e, "z strips");
+        if ((e = cudaMemsetAsync(s.mzv, 0, zbytes, ctx->stream)) != cudaSuccess) return bad(e, "z strips");
     }
-    if (nrec > 0) {
-        if ((e = cudaMalloc(&s.rec, sizeof(int2) * nrec)) != cudaSuccess) return bad(e, "receivers");
-        if ((e = cudaMemcpyAsync(s.rec, hr.data(), sizeof(int2) * nrec, cudaMemcpyHostToDevice, ctx->stream)) !=
-            cudaSuccess)
+    if ((e = cudaMalloc(&s.acc, sizeof(float) * 2)) != cudaSuccess) return bad(e, "acc");
+    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(float) * 2, ctx->stream)) != cudaSuccess) return bad(e, "acc");
+    if ((e = cudaMalloc(&s.rec_start, sizeof(int) * start.size())) != cudaSuccess) return bad(e, "receivers");
+    if ((e = cudaMemcpyAsync(s.rec_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice,
+                             ctx->stream)) != cudaSuccess)
+        return bad(e, "receivers");
+    if (!sorted.empty()) {
+        if ((e = cudaMalloc(&s.rec_sorted, sizeof(int4) * sorted.size())) != cudaSuccess) return bad(e, "receivers");
+        if ((e = cudaMemcpyAsync(s.rec_sorted, sorted.data(), sizeof(int4) * sorted.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream)) != cudaSuccess)
             return bad(e, "receivers");
     }
     s.nrec = nrec;
@@ -436,7 +642,7 @@ int poe_sync(poe_ctx *ctx)
 {
     if (!ctx) return POE_EINVAL;
     CK(cudaStreamSynchronize(ctx->stream));
-    return POE_OK;
+    return device_status(ctx);
 }
 
 int poe_get_traces(poe_ctx *ctx, int32_t shot, float *host_out, int64_t capacity_floats)
@@ -448,8 +654,32 @@ int poe_get_traces(poe_ctx *ctx, int32_t shot, float *host_out, int64_t capacity
     if (!host_out || capacity_floats < n) return fail(ctx, POE_EINVAL, "trace buffer too small");
     CK(cudaMemcpyAsync(host_out, s->trace, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return device_status(ctx);
+}
+
+namespace {
+// plane holding a field of the shot's current state (derived planes are
+// computed into ctx->derived first)
+int field_plane(poe_ctx *ctx, int32_t shot, int32_t field, const float **plane)
+{
+    ShotHost *s = &ctx->shots[shot];
+    const ModelDev &m = ctx->m;
+    const float *cur = s->f[s->steps & 1];
+    static const int map[POE_NFIELDS] = {SF_VX, SF_VZ, SF_WX, SF_WZ, -1, -1, SF_SXZ, -1,
+                                         SF_G11, SF_G22, SF_XI1, SF_XI2};
+    if (map[field] >= 0) {
+        *plane = cur + map[field] * m.plane;
+        return POE_OK;
+    }
+    if (!ctx->derived) CK(cudaMalloc(&ctx->derived, sizeof(float) * 3 * m.plane));
+    int rc;
+    if ((rc = sync_shots(ctx)) != POE_OK) return rc;
+    CKL(launch_derive(m, ctx->shots_dev, shot, s->steps, ctx->derived, ctx->stream));
+    const int which = field == POE_F_SXX ? 0 : (field == POE_F_SZZ ? 1 : 2);
+    *plane = ctx->derived + which * m.plane;
     return POE_OK;
 }
+}  // namespace
 
 int poe_get_field(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out)
 {
@@ -458,10 +688,13 @@ int poe_get_field(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out)
     if (field < 0 || field >= POE_NFIELDS || !host_out) return fail(ctx, POE_EINVAL, "field id");
     const ModelDev &m = ctx->m;
     const int nx = m.NX + 1, nz = m.NZ + 1;
-    CK(cudaMemcpy2DAsync(host_out, sizeof(float) * nx, s->f + field * m.plane + (int64_t)ZH * m.P + XH,
-                         sizeof(float) * m.P, sizeof(float) * nx, nz, cudaMemcpyDeviceToHost, ctx->stream));
+    const float *plane = nullptr;
+    int rc = field_plane(ctx, shot, field, &plane);
+    if (rc != POE_OK) return rc;
+    CK(cudaMemcpy2DAsync(host_out, sizeof(float) * nx, plane + (int64_t)ZH * m.P + XH, sizeof(float) * m.P,
+                         sizeof(float) * nx, nz, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return POE_OK;
+    return device_status(ctx);
 }
 
 int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in)
@@ -469,10 +702,15 @@ int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_i
     ShotHost *s = get_shot(ctx, shot);
     if (!s) return fail(ctx, POE_EINVAL, "shot id");
     if (field < 0 || field >= POE_NFIELDS || !host_in) return fail(ctx, POE_EINVAL, "field id");
+    if (field == POE_F_SXX || field == POE_F_SZZ || field == POE_F_P)
+        return fail(ctx, POE_EINVAL, "sigma_xx, sigma_zz and p are derived from g11 g22 xi1 xi2");
+    static const int map[POE_NFIELDS] = {SF_VX, SF_VZ, SF_WX, SF_WZ, -1, -1, SF_SXZ, -1,
+                                         SF_G11, SF_G22, SF_XI1, SF_XI2};
     const ModelDev &m = ctx->m;
     const int nx = m.NX + 1, nz = m.NZ + 1;
-    CK(cudaMemcpy2DAsync(s->f + field * m.plane + (int64_t)ZH * m.P + XH, sizeof(float) * m.P, host_in,
-                         sizeof(float) * nx, sizeof(float) * nx, nz, cudaMemcpyHostToDevice, ctx->stream));
+    float *plane = s->f[s->steps & 1] + map[field] * m.plane;
+    CK(cudaMemcpy2DAsync(plane + (int64_t)ZH * m.P + XH, sizeof(float) * m.P, host_in, sizeof(float) * nx,
+                         sizeof(float) * nx, nz, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return POE_OK;
 }
@@ -490,9 +728,16 @@ int poe_reset_shot(poe_ctx *ctx, int32_t shot)
     ShotHost *s = get_shot(ctx, shot);
     if (!s) return fail(ctx, POE_EINVAL, "shot id");
     const ModelDev &m = ctx->m;
-    CK(cudaMemsetAsync(s->f, 0, sizeof(float) * m.plane * NSTATE, ctx->stream));
-    if (s->mx) CK(cudaMemsetAsync(s->mx, 0, sizeof(float) * 6 * (size_t)(m.NZ + 1) * m.Wx, ctx->stream));
-    if (s->mz) CK(cudaMemsetAsync(s->mz, 0, sizeof(float) * 6 * (size_t)m.Hz * m.P, ctx->stream));
+    const size_t xbytes = sizeof(float) * 3 * (size_t)(m.NZ + 1) * m.Wx;
+    const size_t zbytes = sizeof(float) * 3 * (size_t)m.Hz * m.P;
+    CK(cudaMemsetAsync(s->f[0], 0, sizeof(float) * m.plane * NSF * 2, ctx->stream));
+    for (int b = 0; b < 2; ++b) {
+        if (s->mx[b]) CK(cudaMemsetAsync(s->mx[b], 0, xbytes, ctx->stream));
+        if (s->mz[b]) CK(cudaMemsetAsync(s->mz[b], 0, zbytes, ctx->stream));
+    }
+    if (s->mxv) CK(cudaMemsetAsync(s->mxv, 0, xbytes, ctx->stream));
+    if (s->mzv) CK(cudaMemsetAsync(s->mzv, 0, zbytes, ctx->stream));
+    CK(cudaMemsetAsync(s->acc, 0, sizeof(float) * 2, ctx->stream));
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(float) * s->trace_cap * s->nrec, ctx->stream));
     s->steps = 0;
     ctx->shots_dirty = true;
@@ -504,8 +749,9 @@ int poe_check_finite(poe_ctx *ctx, int32_t shot, float threshold, float *max_abs
     ShotHost *s = get_shot(ctx, shot);
     if (!s) return fail(ctx, POE_EINVAL, "shot id");
     const ModelDev &m = ctx->m;
-    std::vector<float> h((size_t)m.plane * 8);
-    CK(cudaMemcpyAsync(h.data(), s->f, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<float> h((size_t)m.plane * NSF);
+    CK(cudaMemcpyAsync(h.data(), s->f[s->steps & 1], sizeof(float) * h.size(), cudaMemcpyDeviceToHost,
+                       ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     float mx = 0.0f;
     bool bad = false;
@@ -539,7 +785,11 @@ void poe_destroy(poe_ctx *ctx)
     cudaFree(ctx->coef);
     cudaFree(ctx->px);
     cudaFree(ctx->pz);
-    cudaFree(ctx->scratch);
+    cudaFree(ctx->derived);
+    cudaFree(ctx->err_dev);
+    cudaFree(ctx->ids);
+    cudaFree(ctx->mtab);
+    cudaFree(ctx->tm_ids);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

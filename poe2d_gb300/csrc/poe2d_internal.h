@@ -3,10 +3,10 @@
 //
 // HBM layout of one model (one grid, shared by all its shots):
 //   * every full-grid plane has pitch P floats (a multiple of 32, i.e. 128 B
-//     rows) and R = nz + 2*ZH rows; cell (x, z) sits at (z+ZH)*P + (x+XH).
-//     The XH columns left of x = 0, the columns right of x = NX and the ZH
-//     rows above/below the grid are zero forever, so every 4-point stencil
-//     read stays inside the allocation with no bounds test.  The reference's
+//     rows) and R rows; cell (x, z) sits at (z+ZH)*P + (x+XH).  P and R
+//     cover every tile of the grid plus its 4-cell halo (P >= 64 ntx + 8,
+//     R = 32 ntz + 8), and everything outside the grid is zero forever, so
+//     tile loads and 4-point stencils need no bounds test.  The reference's
 //     one out-of-row read (stress1 at x = NX-1 reads x+2, which with pitch
 //     NX+1 wraps to column 0 of the next row, cu:56) reads a zero here as it
 //     does there: column 0 is never written by any kernel.
@@ -14,11 +14,13 @@
 //   * profiles: 6 x-profiles of length P (index x+XH) and 6 z-profiles of
 //     length R (index z+ZH).
 // Per shot:
-//   * 12 state planes (vx vz wx wz sxx szz sxz p g11 g22 xi1 xi2);
-//   * C-PML memory only on the absorbing strips: the 6 x-direction variables
-//     on columns x < xL or x >= xR (nz x Wx each), the 6 z-direction ones on
-//     rows z < zT or z >= zB (Hz x P each).  Outside the strips the
-//     reference's a = 0 and b = 1, so its memory variables stay exactly zero
+//   * 9 integrated state planes (vx vz wx wz sxz g11 g22 xi1 xi2), twice
+//     (step n reads one set and writes the other); sigma_xx, sigma_zz and
+//     sigma2 = p are pointwise functions of these and are not stored;
+//   * C-PML memory only on the absorbing strips: x-direction variables on
+//     columns x < xL or x >= xR (nz x Wx each), z-direction ones on rows
+//     z < zT or z >= zB (Hz x P each).  Outside the strips the reference's
+//     a = 0 and b = 1, so its memory variables stay exactly zero
 //     (cu:1090-1095, 1152-1158): they are not stored.
 #pragma once
 #include <stdint.h>
@@ -30,13 +32,8 @@ namespace poe {
 constexpr int XH = 4;  // halo columns left of x = 0
 constexpr int ZH = 4;  // halo rows above z = 0 and below z = NZ
 
-enum { NSTATE = 12 };
-enum { F_VX = 0, F_VZ, F_WX, F_WZ, F_SXX, F_SZZ, F_SXZ, F_P, F_G11, F_G22, F_XI1, F_XI2 };
 enum { C_RHO = 0, C_RHOF, C_RSM, C_EOK, C_LC, C_MU, C_AL, C_M };
 enum { PA = 0, PB, PK, PAH, PBH, PKH };
-// memory variables: x-direction (stored on x strips) and z-direction
-enum { MX_SXX = 0, MX_S2, MX_SXZ, MX_VX1, MX_VX2, MX_VZ };   // b/a: xh xh x x x xh
-enum { MZ_SXX = 0, MZ_S2, MZ_SXZ, MZ_VX, MZ_VZ1, MZ_VZ2 };   // b/a: z z zh z zh zh
 enum { SRC_NONE = -1, SRC_P = 0, SRC_FZ = 1 };
 
 struct ModelDev {
@@ -50,22 +47,18 @@ struct ModelDev {
     const float *pz;   // 6 * R
     int xL, xR, Wx;    // x strips: x < xL or x >= xR; Wx = xL + (NX+1 - xR)
     int zT, zB, Hz;    // z strips: z < zT or z >= zB; Hz = zT + (NZ+1 - zB)
+    int *err;          // device flag: a bounded wait in a kernel gave up
+    // palette mode: one byte per cell selects a row of a small material table
+    const uint8_t *ids;      // padded plane of material ids (pitch P bytes, R rows), or null
+    const float *mtab;       // nmat rows of MT_W floats
+    int nmat;
+    const void *tm_ids;      // TMA descriptor of the id plane (device memory)
 };
 
-struct ShotDev {
-    float *f;              // NSTATE planes
-    float *mx;             // 6 * (NZ+1) * Wx
-    float *mz;             // 6 * Hz * P
-    const int64_t *step;   // steps done (device counter)
-    int64_t src_off;       // plane offset of the source cell, or -1
-    int src_where;         // SRC_P / SRC_FZ / SRC_NONE
-    int64_t src_n;         // active steps
-    const float *src_tab;
-    const int2 *rec;       // (plane offset, comp) ; comp < 0: inert
-    int nrec;
-    float *trace;          // [cap][nrec]
-    int64_t trace_cap;
-};
+// material-table row: the 8 coefficient planes' values, then quantities the
+// reference derives from them per cell, rounded as it rounds them
+enum { MT_RHOF_EOK = 8, MT_CO, MT_C1, MT_C2, MT_RCO, MT_RC1, MT_W = 16 };
+constexpr int MAX_PALETTE = 64;
 
 // x-strip column of x, or -1
 __host__ __device__ __forceinline__ int xcol(const ModelDev &m, int x)
@@ -78,14 +71,44 @@ __host__ __device__ __forceinline__ int zrow(const ModelDev &m, int z)
     return z < m.zT ? z : (z >= m.zB ? m.zT + (z - m.zB) : -1);
 }
 
-// kernel launchers (poe2d_kernels.cu); return cudaError_t as int
-// one time step of every shot: stress, record, velocity (k: offset added to
-// each shot's step counter)
-int launch_step(const ModelDev &m, const ShotDev *shots_dev, int nshots, int max_rec, int k,
-                bool exact, bool kone, void *stream);
+// ---- fused tile step (poe2d_tile.cu) ----
+constexpr int TILE_X = 64;   // cells per tile along x
+constexpr int TILE_Z = 32;   // cells per tile along z
+
+// integrated state planes per buffer (sigma_xx, sigma_zz, p are derived)
+enum { SF_VX = 0, SF_VZ, SF_WX, SF_WZ, SF_SXZ, SF_G11, SF_G22, SF_XI1, SF_XI2, NSF };
+// stress C-PML memory (double-buffered) and velocity C-PML memory (in place)
+enum { MXS_SXX = 0, MXS_S2, MXS_SXZ };   // x strips, profiles xh xh x
+enum { MZS_SXX = 0, MZS_S2, MZS_SXZ };   // z strips, profiles z z zh
+enum { MXV_VX1 = 0, MXV_VX2, MXV_VZ };   // x strips, profiles x x xh
+enum { MZV_VX = 0, MZV_VZ1, MZV_VZ2 };   // z strips, profiles z zh zh
+
+struct StreamShot {
+    float *f[2];           // NSF planes each; step n reads f[(n-1)&1], writes f[n&1]
+    float *mx[2], *mz[2];  // 3 stress memory arrays each (nz x Wx / Hz x P)
+    float *mxv, *mzv;      // 3 velocity memory arrays each
+    float *acc;            // [2]: sigma2 at a source cell outside stress1's range
+    const int64_t *step;   // steps done (device counter)
+    int64_t src_off;       // plane offset of the source cell, or -1
+    int src_where;         // SRC_P / SRC_FZ / SRC_NONE
+    int64_t src_n;         // active steps of the source table
+    const float *src_tab;
+    const int *rec_start;  // CSR over tiles: ntiles + 1 entries
+    const int4 *rec_sorted;// (x, comp, slot, z), grouped by tile
+    int nrec;
+    float *trace;          // [cap][nrec]
+    int64_t trace_cap;
+    const void *tm_v;      // TMA descriptors over both state buffers (palette mode)
+    const void *tm_s;
+};
+
+int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, int k, bool exact, bool kone,
+                     void *stream);
+// TMA box sizes of the palette kernel (elements): velocity tile, stress state, ids
+constexpr int TMA_VW = TILE_X + 8, TMA_VH = TILE_Z + 8, TMA_SH = TILE_Z + 4, TMA_IW = TILE_X + 16,
+              TMA_IH = TILE_Z + 5;
+int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream);
 // steps[i] += by for every shot
 int launch_advance(int64_t *steps_dev, int nshots, int64_t by, void *stream);
-// f[0..n) = 0
-int launch_zero(float *f, int64_t n, void *stream);
 
 }  // namespace poe

@@ -1,0 +1,720 @@
+// poe2d_tile.cu -- the fused time step: one launch = stress + velocity.
+//
+// One CTA (256 threads) advances a TX x TZ = 64 x 32 tile of one shot:
+//   1. vx vz wx wz of the tile + 4-cell halo (72 x 40) -> shared memory
+//      (16-byte vector loads, rows 16-B aligned by the padded layout);
+//   2. stress on the tile + 2-cell halo (68 x 36 cells): strains, fluid
+//      content, sigma2 = p, sigma_xz, sigma_xx, sigma_zz (cu:49-112,
+//      202-229, 231-244) -> shared memory; the integrated state of the tile's
+//      own cells -> HBM.  The halo is recomputed so no tile waits for another;
+//   3. receivers of the tile are recorded (before the velocity update, as
+//      save1_kernel runs, cu:1629);
+//   4. velocity on the tile (cu:279-386) -> HBM.
+// sigma_xx, sigma_zz and p never touch HBM.  Tiles re-read this step's inputs
+// in their halos, so the state is double-buffered: step n reads buffer
+// (n-1)&1 and writes buffer n&1 (the stress C-PML memory too; the velocity
+// C-PML memory is per-cell private and updated in place).
+//
+// Arithmetic per cell is the reference's, in the same order, with its FP64
+// sub-expressions rounded as in poe2d_math.cuh (EXACT) or plain FP32
+// stencils (FAST); compiled with -fmad=false.
+#include <cuda_runtime.h>
+
+#include "poe2d_internal.h"
+
+namespace poe {
+
+namespace {
+
+constexpr int TX = TILE_X, TZ = TILE_Z;
+constexpr int VW = TX + 8, VH = TZ + 8;     // velocity tile with halo
+constexpr int SW = TX + 4, SH = TZ + 4;     // stress tile with halo
+constexpr int NT = 256;
+#ifndef STRESS_UNROLL
+#define STRESS_UNROLL 2
+#endif
+#ifndef VEL_UNROLL
+#define VEL_UNROLL 2
+#endif
+constexpr int kStressUnroll = STRESS_UNROLL;   // cells in flight per thread (memory-level parallelism)
+constexpr int kVelUnroll = VEL_UNROLL;
+constexpr int V_FLOATS = VW * VH, S_FLOATS = SW * SH;
+enum { SV_VX = 0, SV_VZ, SV_WX, SV_WZ };
+enum { SS_SXX = 0, SS_SZZ, SS_SXZ, SS_P };
+
+template <bool EXACT>
+__device__ __forceinline__ float D4(float a, float b, float c, float d, const Div24 &q)
+{
+    return EXACT ? d4_exact(a, b, c, d, q) : d4_fast(a, b, c, d, q);
+}
+
+template <bool KONE>
+__device__ __forceinline__ float KDIV(float v, float K)
+{
+    return KONE ? v : v / K;
+}
+
+// ---- mbarrier / TMA primitives (sm_90+ PTX) ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for a phase; false if it did not complete within the limit
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 20); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// the descriptor lives in device memory, written by the host before launch
+__device__ __forceinline__ void tma_prefetch_desc(const void *desc)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(desc) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0, int c1, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// a / b, correctly rounded, from y = RN(1/b) (Markstein 1990: with y the
+// correctly rounded reciprocal and q0 within an ulp of a/b, the residual is
+// exact and q0 + r y rounds to RN(a/b)); valid away from overflow/underflow
+__device__ __forceinline__ float div_by(float a, float b, float y)
+{
+    const float q0 = a * y;
+    const float r = fmaf(-b, q0, a);
+    return fmaf(r, y, q0);
+}
+
+}  // namespace
+
+template <bool EXACT, bool KONE>
+__global__ void __launch_bounds__(NT, 2)
+k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
+{
+    extern __shared__ __align__(16) float sm[];
+    float *sv = sm;                       // 4 x VH x VW
+    float *ss = sm + 4 * V_FLOATS;        // 4 x SH x SW
+    const int tid = threadIdx.x;
+    const int tx = blockIdx.x % ntx, tz = blockIdx.x / ntx;
+    const StreamShot &S = shots[blockIdx.y];
+    const int64_t n = *S.step + k + 1;
+    const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+    const int NX = m.NX, NZ = m.NZ;
+    const int P = m.P;
+    const int64_t PL = m.plane;
+    const int x0 = tx * TX, z0 = tz * TZ;
+    const float dt = m.dt;
+    const float *__restrict__ FA = S.f[rd];
+    float *__restrict__ FB = S.f[wr];
+    const float *__restrict__ C = m.coef;
+    const float *__restrict__ PX = m.px;
+    const float *__restrict__ PZ = m.pz;
+    const int R = m.R;
+    const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
+    const int src_off = (int)S.src_off;
+    const int src_where = S.src_where;
+    const bool src_on = n <= S.src_n;
+    const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
+
+    // ---- 1. velocity tile with halo: columns x0-4 .. x0+TX+3, rows z0-4 .. z0+TZ+3.
+    //         Column x0-4 sits at padded index x0 (XH = 4): 16-B aligned rows.
+    {
+        const int vec_per_row = VW / 4;                  // 18 float4 per row
+        const int total = 4 * VH * vec_per_row;
+#pragma unroll 4
+        for (int i = tid; i < total; i += NT) {
+            const int f = i / (VH * vec_per_row);
+            const int rem = i - f * (VH * vec_per_row);
+            const int zz = rem / vec_per_row, xv = rem - zz * vec_per_row;
+            const float4 v = *reinterpret_cast<const float4 *>(
+                FA + (int64_t)(SF_VX + f) * PL + (int64_t)(z0 - 4 + zz + ZH) * P + x0 + 4 * xv);
+            *reinterpret_cast<float4 *>(sv + f * V_FLOATS + zz * VW + 4 * xv) = v;
+        }
+    }
+    __syncthreads();
+
+    // ---- 2. stress on the tile + 2-cell halo
+    const float pacc = S.acc[rd];
+#pragma unroll kStressUnroll
+    for (int i = tid; i < S_FLOATS; i += NT) {
+        const int zl = i / SW, xl = i - zl * SW;
+        const int x = x0 - 2 + xl, z = z0 - 2 + zl;
+        const int a = xl + 2, b = zl + 2;                 // position in the velocity tile
+        const float *VXs = sv + SV_VX * V_FLOATS + b * VW + a;
+        const float *VZs = sv + SV_VZ * V_FLOATS + b * VW + a;
+        const float *WXs = sv + SV_WX * V_FLOATS + b * VW + a;
+        const float *WZs = sv + SV_WZ * V_FLOATS + b * VW + a;
+        const bool cell_ok = x >= 0 && x <= NX && z >= 0 && z <= NZ;
+        const bool g1 = cell_ok && x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;   // cu:60-62
+        const bool g2 = cell_ok && x >= 2 && x <= NX - 1 && z >= 1 && z <= NZ - 2;   // cu:212-214
+        const bool g3 = cell_ok && x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;   // cu:237-239
+        const bool own = cell_ok && x >= x0 && x < x0 + TX && z >= z0 && z < z0 + TZ;
+        const int o = (z + ZH) * P + (x + XH);
+        // the six stencils (cu:64-65, 76-77, 220-221)
+        const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
+        const float vdz = D4<EXACT>(VZs[0], VZs[-VW], VZs[VW], VZs[-2 * VW], m.qz);
+        const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
+        const float wdz = D4<EXACT>(WZs[0], WZs[-VW], WZs[VW], WZs[-2 * VW], m.qz);
+        const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
+        const float sdz = D4<EXACT>(VXs[VW], VXs[0], VXs[2 * VW], VXs[-VW], m.qz);
+        float g11 = 0.0f, g22 = 0.0f, xi1 = 0.0f, xi2 = 0.0f, sxz = 0.0f;
+        float lc = 0.0f, mu = 0.0f, mu_top = 0.0f, al = 0.0f, M = 0.0f;
+        if (cell_ok) {
+            g11 = FA[SF_G11 * PL + o];
+            g22 = FA[SF_G22 * PL + o];
+            xi1 = FA[SF_XI1 * PL + o];
+            xi2 = FA[SF_XI2 * PL + o];
+            sxz = FA[SF_SXZ * PL + o];
+            lc = C[C_LC * PL + o];
+            mu = C[C_MU * PL + o];
+            mu_top = C[C_MU * PL + o + P];               // rmu[top] (cu:218)
+            al = C[C_AL * PL + o];
+            M = C[C_M * PL + o];
+        }
+        const int xc = cell_ok ? xcol(m, x) : -1;
+        const int zr = cell_ok ? zrow(m, z) : -1;
+        const int xi = x + XH, zi = z + ZH;
+        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+        if (xc >= 0 && (g1 || g2)) {
+            const int ix = z * Wx + xc;
+            const float *MA = S.mx[rd];
+            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
+            m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
+            m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
+            m5 = PX[PB * P + xi] * MA[MXS_SXZ * nzx + ix] + PX[PA * P + xi] * sdx;
+            if (own) {
+                float *MB = S.mx[wr];
+                if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
+                if (g2) MB[MXS_SXZ * nzx + ix] = m5;
+            }
+        }
+        if (zr >= 0 && (g1 || g2)) {
+            const int iz = zr * P + xi;
+            const float *MA = S.mz[rd];
+            const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
+            m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
+            m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
+            m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
+            if (own) {
+                float *MB = S.mz[wr];
+                if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
+                if (g2) MB[MZS_SXZ * hzp + iz] = m6;
+            }
+        }
+        const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+        const float Kx = KONE ? 1.0f : PX[PK * P + xi];
+        const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
+        if (g1) {   // cu:71-86
+            g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
+            g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
+            xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
+            xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
+        }
+        float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
+        const bool is_src = cell_ok && o == src_off;
+        if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
+        if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
+        if (is_src && own) S.acc[wr] = pv;
+        if (g2) {   // cu:223-226
+            const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
+            sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
+        }
+        float sxx = 0.0f, szz = 0.0f;
+        if (g3) {   // cu:241-242
+            if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
+            else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
+        }
+        ss[SS_SXX * S_FLOATS + i] = sxx;
+        ss[SS_SZZ * S_FLOATS + i] = szz;
+        ss[SS_SXZ * S_FLOATS + i] = sxz;
+        ss[SS_P * S_FLOATS + i] = pv;
+        if (own) {
+            FB[SF_G11 * PL + o] = g11;
+            FB[SF_G22 * PL + o] = g22;
+            FB[SF_XI1 * PL + o] = xi1;
+            FB[SF_XI2 * PL + o] = xi2;
+            FB[SF_SXZ * PL + o] = sxz;
+        }
+    }
+    __syncthreads();
+
+    // ---- 3. receivers of this tile (vx, vz before the update; p of this step)
+    if (S.nrec > 0 && n <= S.trace_cap) {
+        const int tile = tz * ntx + tx;
+        const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
+        float *trace_row = S.trace + (n - 1) * S.nrec;
+        for (int q = qb + tid; q < qe; q += NT) {
+            const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
+            const int xl = Rq.x - x0, zl = Rq.w - z0;
+            float v;
+            if (Rq.y == 2) v = ss[SS_P * S_FLOATS + (zl + 2) * SW + xl + 2];
+            else v = sv[(Rq.y == 0 ? SV_VX : SV_VZ) * V_FLOATS + (zl + 4) * VW + xl + 4];
+            trace_row[Rq.z] = v;
+        }
+    }
+
+    // ---- 4. velocity on the tile
+    float *__restrict__ MXV = S.mxv;
+    float *__restrict__ MZV = S.mzv;
+#pragma unroll kVelUnroll
+    for (int i = tid; i < TX * TZ; i += NT) {
+        const int zl = i / TX, xl = i - zl * TX;
+        const int x = x0 + xl, t = z0 + zl;
+        if (x > NX || t > NZ) continue;
+        const int c = xl + 2, d = zl + 2;                // position in the stress tile
+        const float *SXX = ss + SS_SXX * S_FLOATS + d * SW + c;
+        const float *SZZ = ss + SS_SZZ * S_FLOATS + d * SW + c;
+        const float *SXZ = ss + SS_SXZ * S_FLOATS + d * SW + c;
+        const float *PP = ss + SS_P * S_FLOATS + d * SW + c;
+        const int vo = (zl + 4) * VW + xl + 4;
+        const float vx0 = sv[SV_VX * V_FLOATS + vo], vz0 = sv[SV_VZ * V_FLOATS + vo];
+        const float wx0 = sv[SV_WX * V_FLOATS + vo], wz0 = sv[SV_WZ * V_FLOATS + vo];
+        const int o = (t + ZH) * P + (x + XH);
+        const int xi = x + XH, zi = t + ZH;
+        // the six stencils (cu:297-299, 342-344)
+        const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
+        const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
+        const float d3x = D4<EXACT>(SXZ[0], SXZ[-SW], SXZ[SW], SXZ[-2 * SW], m.qz);
+        const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
+        const float d2z = D4<EXACT>(SZZ[SW], SZZ[0], SZZ[2 * SW], SZZ[-SW], m.qz);
+        const float d3z = D4<EXACT>(PP[SW], PP[0], PP[2 * SW], PP[-SW], m.qz);
+        const bool gvx = x >= 2 && x <= NX - 1 && t >= 2 && t <= NZ - 1;   // cu:289-291
+        const bool gvz = x >= 1 && x <= NX - 2 && t >= 1 && t <= NZ - 2;   // cu:326-328
+        const int xc = xcol(m, x), zr = zrow(m, t);
+        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+        if (xc >= 0 && (gvx || gvz)) {
+            const int ix = t * Wx + xc;
+            float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix, *M4 = MXV + MXV_VZ * nzx + ix;
+            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
+            m1 = bx * *M1 + ax * d1x;
+            m2 = bx * *M2 + ax * d2x;
+            m4 = PX[PBH * P + xi] * *M4 + PX[PAH * P + xi] * d1z;
+            if (gvx) { *M1 = m1; *M2 = m2; }
+            if (gvz) *M4 = m4;
+        }
+        if (zr >= 0 && (gvx || gvz)) {
+            const int iz = zr * P + xi;
+            float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz, *M6 = MZV + MZV_VZ2 * hzp + iz;
+            const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
+            m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
+            m5 = bh * *M5 + ah * d2z;
+            m6 = bh * *M6 + ah * d3z;
+            if (gvx) *M3 = m3;
+            if (gvz) { *M5 = m5; *M6 = m6; }
+        }
+        const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+        const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
+        float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
+        if (gvx) {   // material at (x, t), cu:293-311
+            const float rho = C[C_RHO * PL + o], rhof = C[C_RHOF * PL + o];
+            const float rsm = C[C_RSM * PL + o], eok = C[C_EOK * PL + o];
+            const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
+            const float B = KDIV<KONE>(d2x, Kx) + m2;
+            const float co = (rho * rsm - rhof * rhof) / dt;
+            const float c1 = co + rho * eok * 0.5f;
+            const float c2 = co - rho * eok * 0.5f;
+            wx1 = (c2 * wx0 + (-rhof * A - rho * B)) / c1;
+            vx1 = vx0 + (rsm * A + rhof * B + rhof * eok * ((wx0 + wx1) * 0.5f)) / co;
+        }
+        if (gvz) {   // material at (x, t+1), cu:330-353
+            const int op = o + P;
+            const float rho = C[C_RHO * PL + op], rhof = C[C_RHOF * PL + op];
+            const float rsm = C[C_RSM * PL + op], eok = C[C_EOK * PL + op];
+            float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
+            const float B = KDIV<KONE>(d3z, Kzh) + m6;
+            if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
+            const float co = (rho * rsm - rhof * rhof) / dt;
+            const float c1 = co + rho * eok * 0.5f;
+            const float c2 = co - rho * eok * 0.5f;
+            wz1 = (c2 * wz0 + (-rhof * A - rho * B)) / c1;
+            vz1 = vz0 + (rsm * A + rhof * B + rhof * eok * ((wz0 + wz1) * 0.5f)) / co;
+        }
+        FB[SF_VX * PL + o] = vx1;
+        FB[SF_WX * PL + o] = wx1;
+        FB[SF_VZ * PL + o] = vz1;
+        FB[SF_WZ * PL + o] = wz1;
+    }
+}
+
+
+// ===================================================================== palette
+// Same step as k_tile for models whose 8 coefficient planes take at most
+// MAX_PALETTE distinct values (patchy models: 2): each cell carries a one-byte
+// material id and every per-cell coefficient the reference computes (co, c1,
+// c2, rhof*eta/kappa, 1/co, 1/c1) comes from a table row in shared memory.
+// All of the tile's inputs (velocity tile + halo, stress state + halo, ids)
+// arrive by TMA in one batch before any computation, so the compute phases
+// read only shared memory.
+namespace {
+constexpr int PV_FLOATS = TMA_VW * TMA_VH;       // 72 x 40
+constexpr int PS_FLOATS = TMA_VW * TMA_SH;       // 72 x 36
+constexpr int PI_BYTES = TMA_IW * TMA_IH;        // 80 x 37
+constexpr int PAL_OFF_S = 4 * PV_FLOATS * 4;
+constexpr int PAL_OFF_I = PAL_OFF_S + 5 * PS_FLOATS * 4;
+constexpr int PAL_OFF_T = PAL_OFF_I + (PI_BYTES + 127) / 128 * 128;
+constexpr int PAL_OFF_B = PAL_OFF_T + MAX_PALETTE * MT_W * 4;
+constexpr size_t PAL_SMEM = PAL_OFF_B + 16;
+constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_FLOATS * 4 + PI_BYTES;
+static_assert(PAL_OFF_S % 128 == 0 && PAL_OFF_I % 128 == 0 && PAL_OFF_T % 128 == 0, "TMA smem alignment");
+static_assert((PV_FLOATS * 4) % 128 == 0 && (PS_FLOATS * 4) % 128 == 0, "TMA smem alignment");
+// state slots in shared memory; after the stress phase they hold its outputs
+enum { PS_G11 = 0, PS_G22, PS_XI1, PS_XI2, PS_SXZ };
+enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
+}  // namespace
+
+template <bool EXACT, bool KONE>
+__global__ void __launch_bounds__(NT, 2)
+k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
+{
+    extern __shared__ __align__(128) unsigned char smp[];
+    float *sv = reinterpret_cast<float *>(smp);                 // 4 x 40 x 72, from (x0-4, z0-4)
+    float *ss = reinterpret_cast<float *>(smp + PAL_OFF_S);     // 5 x 36 x 72, from (x0-4, z0-2)
+    const uint8_t *si = smp + PAL_OFF_I;                         // 37 x 80,     from (x0-4, z0-2)
+    float *st = reinterpret_cast<float *>(smp + PAL_OFF_T);     // nmat x MT_W
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
+    const int tid = threadIdx.x;
+    const int tx = blockIdx.x % ntx, tz = blockIdx.x / ntx;
+    const StreamShot &S = shots[blockIdx.y];
+    const int64_t n = *S.step + k + 1;
+    const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+    const int NX = m.NX, NZ = m.NZ;
+    const int P = m.P;
+    const int64_t PL = m.plane;
+    const int x0 = tx * TX, z0 = tz * TZ;
+    const float dt = m.dt;
+    float *__restrict__ FB = S.f[wr];
+    const float *__restrict__ PX = m.px;
+    const float *__restrict__ PZ = m.pz;
+    const int R = m.R;
+    const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
+    const int src_off = (int)S.src_off;
+    const int src_where = S.src_where;
+    const bool src_on = n <= S.src_n;
+    const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
+
+    // ---- 1. one batch of TMA loads: 4 velocity planes, 5 state planes, ids
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_expect_tx(bar, PAL_TX_BYTES);
+        const int cv = rd * NSF;
+        for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, bar);
+        const int sp[5] = {SF_G11, SF_G22, SF_XI1, SF_XI2, SF_SXZ};
+        for (int f = 0; f < 5; ++f) tma_load_3d(ss + f * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + sp[f], bar);
+        tma_load_2d(const_cast<uint8_t *>(si), m.tm_ids, x0, z0 + 2, bar);
+    }
+    for (int i = tid; i < m.nmat * MT_W; i += NT) st[i] = m.mtab[i];
+    const float pacc = S.acc[rd];
+    __syncthreads();                                    // table visible
+    if (!mbar_wait(bar, 0)) {                           // bounded: report and leave
+        if (tid == 0) atomicExch(m.err, 1);
+        return;
+    }
+
+    // ---- 2. stress on the tile + 2-cell halo (68 x 36)
+    for (int i = tid; i < S_FLOATS; i += NT) {
+        const int zl = i / SW, xl = i - zl * SW;
+        const int x = x0 - 2 + xl, z = z0 - 2 + zl;
+        const int vo = (zl + 2) * TMA_VW + xl + 2;      // in the velocity tile
+        const int so = zl * TMA_VW + xl + 2;            // in the state tile
+        const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
+        const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
+        const bool cell_ok = x >= 0 && x <= NX && z >= 0 && z <= NZ;
+        const bool g1 = cell_ok && x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;   // cu:60-62
+        const bool g2 = cell_ok && x >= 2 && x <= NX - 1 && z >= 1 && z <= NZ - 2;   // cu:212-214
+        const bool g3 = cell_ok && x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;   // cu:237-239
+        const bool own = cell_ok && x >= x0 && x < x0 + TX && z >= z0 && z < z0 + TZ;
+        const int o = (z + ZH) * P + (x + XH);
+        const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
+        const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
+        const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
+        const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
+        const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
+        const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
+        float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
+        float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
+        float sxz = ss[PS_SXZ * PS_FLOATS + so];
+        const float *mt = st + MT_W * si[zl * TMA_IW + xl + 2];
+        const float *mtop = st + MT_W * si[(zl + 1) * TMA_IW + xl + 2];
+        const float lc = mt[C_LC], mu = mt[C_MU], al = mt[C_AL], M = mt[C_M];
+        const float mu_top = mtop[C_MU];                 // rmu[top] (cu:218)
+        const int xc = cell_ok ? xcol(m, x) : -1;
+        const int zr = cell_ok ? zrow(m, z) : -1;
+        const int xi = x + XH, zi = z + ZH;
+        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+        if (xc >= 0 && (g1 || g2)) {
+            const int ix = z * Wx + xc;
+            const float *MA = S.mx[rd];
+            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
+            m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
+            m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
+            m5 = PX[PB * P + xi] * MA[MXS_SXZ * nzx + ix] + PX[PA * P + xi] * sdx;
+            if (own) {
+                float *MB = S.mx[wr];
+                if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
+                if (g2) MB[MXS_SXZ * nzx + ix] = m5;
+            }
+        }
+        if (zr >= 0 && (g1 || g2)) {
+            const int iz = zr * P + xi;
+            const float *MA = S.mz[rd];
+            const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
+            m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
+            m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
+            m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
+            if (own) {
+                float *MB = S.mz[wr];
+                if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
+                if (g2) MB[MZS_SXZ * hzp + iz] = m6;
+            }
+        }
+        const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+        const float Kx = KONE ? 1.0f : PX[PK * P + xi];
+        const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
+        if (g1) {   // cu:71-86
+            g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
+            g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
+            xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
+            xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
+        }
+        float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
+        const bool is_src = cell_ok && o == src_off;
+        if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
+        if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
+        if (is_src && own) S.acc[wr] = pv;
+        if (g2) {   // cu:223-226
+            const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
+            sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
+        }
+        float sxx = 0.0f, szz = 0.0f;
+        if (g3) {   // cu:241-242
+            if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
+            else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
+        }
+        if (own) {
+            FB[SF_G11 * PL + o] = g11;
+            FB[SF_G22 * PL + o] = g22;
+            FB[SF_XI1 * PL + o] = xi1;
+            FB[SF_XI2 * PL + o] = xi2;
+            FB[SF_SXZ * PL + o] = sxz;
+        }
+        // this thread alone reads these slots of this cell: outputs overwrite inputs
+        ss[PO_SXX * PS_FLOATS + so] = sxx;
+        ss[PO_SZZ * PS_FLOATS + so] = szz;
+        ss[PO_P * PS_FLOATS + so] = pv;
+        ss[PO_SXZ * PS_FLOATS + so] = sxz;
+    }
+    __syncthreads();
+
+    // ---- 3. receivers of this tile (vx, vz before the update; p of this step)
+    if (S.nrec > 0 && n <= S.trace_cap) {
+        const int tile = tz * ntx + tx;
+        const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
+        float *trace_row = S.trace + (n - 1) * S.nrec;
+        for (int q = qb + tid; q < qe; q += NT) {
+            const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
+            const int xl = Rq.x - x0, zl = Rq.w - z0;
+            float v;
+            if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
+            else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
+            trace_row[Rq.z] = v;
+        }
+    }
+
+    // ---- 4. velocity on the tile (64 x 32)
+    float *__restrict__ MXV = S.mxv;
+    float *__restrict__ MZV = S.mzv;
+    for (int i = tid; i < TX * TZ; i += NT) {
+        const int zl = i / TX, xl = i - zl * TX;
+        const int x = x0 + xl, t = z0 + zl;
+        if (x > NX || t > NZ) continue;
+        const int so = (zl + 2) * TMA_VW + xl + 4;      // (x, t) in the stress tile
+        const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
+        const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
+        const int vo = (zl + 4) * TMA_VW + xl + 4;
+        const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
+        const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
+        const int o = (t + ZH) * P + (x + XH);
+        const int xi = x + XH, zi = t + ZH;
+        const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
+        const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
+        const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
+        const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
+        const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
+        const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
+        const bool gvx = x >= 2 && x <= NX - 1 && t >= 2 && t <= NZ - 1;   // cu:289-291
+        const bool gvz = x >= 1 && x <= NX - 2 && t >= 1 && t <= NZ - 2;   // cu:326-328
+        const int xc = xcol(m, x), zr = zrow(m, t);
+        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+        if (xc >= 0 && (gvx || gvz)) {
+            const int ix = t * Wx + xc;
+            float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix, *M4 = MXV + MXV_VZ * nzx + ix;
+            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
+            m1 = bx * *M1 + ax * d1x;
+            m2 = bx * *M2 + ax * d2x;
+            m4 = PX[PBH * P + xi] * *M4 + PX[PAH * P + xi] * d1z;
+            if (gvx) { *M1 = m1; *M2 = m2; }
+            if (gvz) *M4 = m4;
+        }
+        if (zr >= 0 && (gvx || gvz)) {
+            const int iz = zr * P + xi;
+            float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz, *M6 = MZV + MZV_VZ2 * hzp + iz;
+            const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
+            m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
+            m5 = bh * *M5 + ah * d2z;
+            m6 = bh * *M6 + ah * d3z;
+            if (gvx) *M3 = m3;
+            if (gvz) { *M5 = m5; *M6 = m6; }
+        }
+        const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+        const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
+        float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
+        {   // vx, wx, material at (x, t) (cu:293-311)
+            const float *mt = st + MT_W * si[(zl + 2) * TMA_IW + xl + 4];
+            const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
+            const float B = KDIV<KONE>(d2x, Kx) + m2;
+            const float w1 = div_by(mt[MT_C2] * wx0 + (-mt[C_RHOF] * A - mt[C_RHO] * B), mt[MT_C1], mt[MT_RC1]);
+            const float v1 = vx0 + div_by(mt[C_RSM] * A + mt[C_RHOF] * B + mt[MT_RHOF_EOK] * ((wx0 + w1) * 0.5f),
+                                          mt[MT_CO], mt[MT_RCO]);
+            if (gvx) { wx1 = w1; vx1 = v1; }
+        }
+        {   // vz, wz, material at (x, t+1) (cu:330-353)
+            const float *mt = st + MT_W * si[(zl + 3) * TMA_IW + xl + 4];
+            float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
+            const float B = KDIV<KONE>(d3z, Kzh) + m6;
+            if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
+            const float w1 = div_by(mt[MT_C2] * wz0 + (-mt[C_RHOF] * A - mt[C_RHO] * B), mt[MT_C1], mt[MT_RC1]);
+            const float v1 = vz0 + div_by(mt[C_RSM] * A + mt[C_RHOF] * B + mt[MT_RHOF_EOK] * ((wz0 + w1) * 0.5f),
+                                          mt[MT_CO], mt[MT_RCO]);
+            if (gvz) { wz1 = w1; vz1 = v1; }
+        }
+        FB[SF_VX * PL + o] = vx1;
+        FB[SF_WX * PL + o] = wx1;
+        FB[SF_VZ * PL + o] = vz1;
+        FB[SF_WZ * PL + o] = wz1;
+    }
+}
+
+namespace {
+constexpr size_t TILE_SMEM = sizeof(float) * (4 * V_FLOATS + 4 * S_FLOATS);
+
+template <bool EXACT, bool KONE>
+int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, int k, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tile<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TILE_SMEM);
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAL_SMEM);
+        attr = true;
+    }
+    const int ntx = (m.NX + 1 + TX - 1) / TX, ntz = (m.NZ + 1 + TZ - 1) / TZ;
+    dim3 grd(ntx * ntz, nshots);
+    if (m.ids) k_tile_pal<EXACT, KONE><<<grd, NT, PAL_SMEM, st>>>(m, shots, k, ntx);
+    else k_tile<EXACT, KONE><<<grd, NT, TILE_SMEM, st>>>(m, shots, k, ntx);
+    return (int)cudaGetLastError();
+}
+}  // namespace
+
+int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, int k, bool exact, bool kone,
+                     void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (exact) return kone ? tile_impl<true, true>(m, shots_dev, nshots, k, st)
+                           : tile_impl<true, false>(m, shots_dev, nshots, k, st);
+    return kone ? tile_impl<false, true>(m, shots_dev, nshots, k, st)
+                : tile_impl<false, false>(m, shots_dev, nshots, k, st);
+}
+
+// ---- small helpers: step counters and derived fields ----
+__global__ void k_advance(int64_t *steps, int nshots, int64_t by)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nshots) steps[i] += by;
+}
+
+int launch_advance(int64_t *steps_dev, int nshots, int64_t by, void *stream)
+{
+    k_advance<<<(nshots + 127) / 128, 128, 0, (cudaStream_t)stream>>>(steps_dev, nshots, by);
+    return (int)cudaGetLastError();
+}
+
+// sigma_xx, sigma_zz, p of a shot's current state (they are not stored by the
+// step kernel); n = steps done, the source term of step n is included.
+__global__ void k_derive(const ModelDev m, const StreamShot *__restrict__ shots, int shot, int64_t n, float *out)
+{
+    const StreamShot &S = shots[shot];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = blockIdx.y;
+    if (x > m.NX || z > m.NZ) return;
+    const int NX = m.NX, NZ = m.NZ;
+    const int64_t P = m.P, PL = m.plane;
+    const int64_t o = (int64_t)(z + ZH) * P + (x + XH);
+    const float *F = S.f[n & 1];
+    auto coef = [&](int c) { return m.ids ? m.mtab[MT_W * m.ids[o] + c] : m.coef[c * PL + o]; };
+    const bool g1 = x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;
+    const bool g3 = x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;
+    const float g11 = F[SF_G11 * PL + o], g22 = F[SF_G22 * PL + o];
+    const float al = coef(C_AL), M = coef(C_M);
+    float pv = 0.0f;
+    if (g1) pv = -al * M * (g11 + g22) + M * (F[SF_XI1 * PL + o] + F[SF_XI2 * PL + o]);
+    const bool is_src = o == S.src_off;
+    if (is_src) {
+        if (!g1) pv = S.acc[n & 1];
+        else if (S.src_where == SRC_P && n >= 1 && n <= S.src_n) pv = pv + S.src_tab[n - 1];
+    }
+    float sxx = 0.0f, szz = 0.0f;
+    if (g3) sxx_szz_exact(coef(C_LC), coef(C_MU), g11, g22, al, pv, sxx, szz);
+    out[0 * PL + o] = sxx;
+    out[1 * PL + o] = szz;
+    out[2 * PL + o] = pv;
+}
+
+int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream)
+{
+    dim3 grd((m.NX + 1 + 127) / 128, m.NZ + 1);
+    k_derive<<<grd, 128, 0, (cudaStream_t)stream>>>(m, shots_dev, shot, n, out);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace poe

@@ -118,10 +118,11 @@ class Solver:
 
     coef: (8, NZ+1, NX+1) float32; prof_x / prof_z from pml_profiles().
     stream: an integer cudaStream_t handle (e.g. torch.cuda.current_stream().cuda_stream)
-    or None for a private stream.  fast=True selects plain FP32 stencils.
+    or None for a private stream.  fast=True selects plain FP32 stencils;
+    palette=False keeps the 8 coefficient planes even for few-material models.
     """
 
-    def __init__(self, g, coef, prof_x, prof_z, stream=None, fast=False):
+    def __init__(self, g, coef, prof_x, prof_z, stream=None, fast=False, palette=True):
         self.g = g
         self.shape = (g.NZ + 1, g.NX + 1)
         coef = np.ascontiguousarray(coef, np.float32)
@@ -131,7 +132,8 @@ class Solver:
             raise PoeError(L.POE_EINVAL, "array sizes do not match the grid")
         h = C.c_void_p()
         check(L.lib().poe_create(C.byref(g), _f(coef), _f(px), _f(pz), C.c_void_p(stream or 0),
-                                 L.CTX_FAST_STENCIL if fast else 0, C.byref(h)))
+                                 (L.CTX_FAST_STENCIL if fast else 0) | (0 if palette else L.CTX_NO_PALETTE),
+                                 C.byref(h)))
         self.h = h
         self.nrec = []
 

@@ -112,6 +112,47 @@ def test_reset_reproduces_and_fields_roundtrip(poe, oracle_mod):
         assert np.array_equal(s.field("wz"), v)
         st, mx = s.check_finite(0)
         assert st == 0 and mx > 0
-        s.set_field("p", np.full((NZ + 1, NX + 1), np.nan, np.float32))
+        with pytest.raises(poe.PoeError):
+            s.set_field("p", v)          # derived from g11 g22 xi1 xi2, not settable
+        s.set_field("sxz", np.full((NZ + 1, NX + 1), np.nan, np.float32))
         st, _ = s.check_finite(0)
         assert st == 3
+
+
+def _patchy(poe, NX, NZ, seed):
+    from poe2d_gb300.patchy import random_patches
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = poe.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    gas = poe.biot_material(rho_f=100.0, k_f=0.02e9, eta=1e-5, **frame)
+    ids = random_patches((NZ + 1, NX + 1), 0.5, fraction=0.2, r_min=1.0, r_max=4.0, seed=seed)
+    return poe.coeffs_biot([water, gas], ids)
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_palette_path_matches_planes_and_oracle(poe, oracle_mod, fast):
+    """A two-material patchy model runs on the palette kernel (one byte per
+    cell, TMA-staged tiles); the same model with palette=False runs on the
+    coefficient-plane kernel.  Both must agree bit for bit, and with the oracle."""
+    O = oracle_mod
+    NX, NZ, dx, dt, f0, n = 130, 97, 0.5, 5e-5, 200.0, 140
+    coef, vp = _patchy(poe, NX, NZ, 5)
+    g = poe.grid(NX, NZ, dx, dt)
+    px, pz = poe.pml_profiles(g, 12, f0, vp)
+    rec = [(x, 15, c) for c in (0, 1, 2) for x in range(14, 120, 13)]
+    src = poe.source(64, 50, poe.SRC_RICKER_FZ, f0, 1e3, 0.0)
+    out = {}
+    for pal in (True, False):
+        with poe.Solver(g, coef, px, pz, fast=fast, palette=pal) as s:
+            s.add_shot(src, rec)
+            s.run(n)
+            out[pal] = (s.traces(), s.field("vz"), s.field("p"), s.field("sxx"))
+    for a, b in zip(out[True], out[False]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    o = O.Oracle(O.F32 if fast else O.REFMIXED, NX, NZ, dx, dx, dt, coef, px, pz)
+    o.set_source(64, 50, O.SRC_FZ, O.source_table(1, f0, dt, n, amplitude=1e3, t_cut=0.0, dx=dx, dz=dx))
+    o.set_receivers(rec)
+    ref = o.run(n)
+    tol = TOL_FAST if fast else TOL_EXACT
+    assert rel_l2(out[True][0], ref) <= tol
+    r = o.field("vz")
+    assert max_rel_peak(out[True][1], r, np.abs(r).max()) <= 10 * tol
