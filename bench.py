@@ -67,12 +67,16 @@ def workload(seed=0, shift=0):
     return g, coef, px, pz, src, rec, ids
 
 
-def alg_bytes_per_step(g, s_ctx_strips):
-    """96 B per cell (8 state fields read+written, 8 coefficients read) plus
-    8 B per C-PML memory variable on its strip (6 x-strip, 6 z-strip)."""
+def alg_bytes_per_step(g, s_ctx_strips, per_cell=96):
+    """Algorithmic HBM bytes of one time step: per_cell bytes per cell plus
+    8 B per C-PML memory variable on its strip (6 on x strips, 6 on z strips).
+    per_cell = 96: 8 FP32 state fields read+written + 8 coefficient planes read.
+    per_cell = 73: what the palette kernel must move at least -- the 9
+    integrated state fields (vx vz wx wz sigma_xz g11 g22 xi1 xi2) read and
+    written (72 B) and a 1-byte material id."""
     nx, nz = g.NX + 1, g.NZ + 1
     wx, hz = s_ctx_strips
-    return 96 * nx * nz + 48 * nz * wx + 48 * nx * hz
+    return per_cell * nx * nz + 48 * nz * wx + 48 * nx * hz
 
 
 def strip_extent(px, pz):
@@ -216,6 +220,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--stencil", default="fast", choices=["fast", "exact"],
+                    help="fast: plain FP32 stencils; exact: FP32 arithmetic rounded like the reference's FP64 lines")
+    ap.add_argument("--no-parity", action="store_true", help="skip the fast-vs-exact drift check")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -234,8 +241,13 @@ def main():
     B.build()
 
     g, coef, px, pz, src, rec, ids = workload(seed=0, shift=8 * rank)
-    stream = torch.cuda.current_stream()
-    solver = P.Solver(g, coef, px, pz, stream=stream.cuda_stream)
+    # a real (non-default) stream: the solver's kernels and the timing events
+    # must be on the same stream (handle 0 would give the solver a private one)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
+    fast = args.stencil == "fast"
+    solver = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=fast)
     solver.add_shot(src, rec)
     cells = (g.NX + 1) * (g.NZ + 1)
 
@@ -273,6 +285,7 @@ def main():
     # roofline of the time step: algorithmic bytes per step / time per step
     hbm, peak_kind = peaks()
     alg = alg_bytes_per_step(g, strip_extent(px, pz))
+    alg_pal = alg_bytes_per_step(g, strip_extent(px, pz), per_cell=73)
     step_s = ms * 1e-3 / (args.steps * NSTEPS)
     achieved = alg / step_s / 1e9
     traffic = None
@@ -284,6 +297,22 @@ def main():
         pass
     trace = solver.traces()
     ok = bool(np.isfinite(trace).all() and np.abs(trace).max() > 0)
+
+    # drift of this run's traces against the other stencil rounding, same shot
+    parity = None
+    if not args.no_parity:
+        other = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=not fast)
+        other.add_shot(src, rec)
+        other.run(NSTEPS)
+        tr2 = other.traces()
+        other.close()
+        comp = {}
+        for ci, name in enumerate(("vx", "vz", "p")):
+            a = trace[:, ci * NREC:(ci + 1) * NREC].astype(np.float64)
+            b = tr2[:, ci * NREC:(ci + 1) * NREC].astype(np.float64)
+            comp[name] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        parity = {"rel_l2_vs_" + ("exact" if fast else "fast") + "_stencils": comp, "tolerance": 1e-5,
+                  "steps": NSTEPS}
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -298,7 +327,7 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            s2 = P.Solver(g, hcoef, px, pz, stream=stream.cuda_stream)
+            s2 = P.Solver(g, hcoef, px, pz, stream=stream.cuda_stream, fast=fast)
             s2.add_shot(src, rec)
             s2.run(NSTEPS)
             P._lib.check(P.lib().poe_get_traces(s2.h, 0, htr.ctypes.data_as(P.solver._fp), htr.size), s2.h)
@@ -329,12 +358,16 @@ def main():
                        "grid": [g.NX + 1, g.NZ + 1], "time_steps": NSTEPS, "pml": NPML, "receivers": NREC,
                        "gas_fraction": float(ids.mean()), "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (12 state planes x 16 MB + 8 coefficient planes)",
-                       "stencil_rounding": "exact (FP64 sub-expressions of the reference rounded once)"},
+                       "stencil_rounding": ("plain FP32 stencils" if fast else
+                                            "exact: FP64 sub-expressions of the reference rounded once"),
+                       "coefficients": "material palette (1-byte id per cell, 2 materials)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_step": alg, "step_us": step_s * 1e6},
+                         "algorithmic_bytes_per_step": alg, "step_us": step_s * 1e6,
+                         "palette_min_bytes_per_step": alg_pal,
+                         "palette_frac": alg_pal / step_s / 1e9 / hbm},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "wall_s": wall, "finite": ok,
+            "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity,
         }
         print(json.dumps(line), flush=True)
     if pg:

@@ -65,9 +65,9 @@ struct poe_ctx {
     int *err_dev = nullptr;     // set by a kernel whose bounded wait gave up
     uint8_t *ids = nullptr;     // palette mode: material id plane
     float *mtab = nullptr;      // palette mode: material table
-    CUtensorMap *tm_ids = nullptr;
     int nmat = 0;
     int ntx = 1, ntz = 1;       // tiles across x and z
+    int tile_x = TILE_X, tile_z = TILE_Z;
     std::string err;
 };
 
@@ -331,19 +331,6 @@ bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool encode_ids(CUtensorMap *out, uint8_t *base, const ModelDev &m)
-{
-    EncodeTiledFn fn = encode_fn();
-    if (!fn) return false;
-    cuuint64_t dims[2] = {(cuuint64_t)m.P, (cuuint64_t)m.R};
-    cuuint64_t strides[1] = {(cuuint64_t)m.P};
-    cuuint32_t box[2] = {(cuuint32_t)TMA_IW, (cuuint32_t)TMA_IH};
-    cuuint32_t es[2] = {1, 1};
-    return fn(out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 // Palette of the coefficient planes: ids (one byte per cell) and table rows
 // holding the 8 coefficients plus what the reference derives from them per
 // cell, with the reference's float operations (cu:293-295, 311).  False if
@@ -374,14 +361,24 @@ bool build_palette(const float *coef, int64_t ncell, float dt, std::vector<uint8
         for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&t[c], &keys[i][c], 4);
         const float rho = t[POE_C_RHO], rhof = t[POE_C_RHOF], rsm = t[POE_C_RSM], eok = t[POE_C_EOK];
         const float co = (rho * rsm - rhof * rhof) / dt;
-        t[MT_RHOF_EOK] = rhof * eok;
-        t[MT_CO] = co;
-        t[MT_C1] = co + rho * eok * 0.5f;
-        t[MT_C2] = co - rho * eok * 0.5f;
-        t[MT_RCO] = (float)(1.0 / (double)co);
-        t[MT_RC1] = (float)(1.0 / (double)t[MT_C1]);
-        if (!std::isfinite(t[MT_RCO]) || !std::isfinite(t[MT_RC1]) || !std::isnormal(co) ||
-            !std::isnormal(t[MT_C1]))
+        float row[MT_W] = {0};
+        row[MT_LC] = t[POE_C_LAMBDAC];
+        row[MT_MU] = t[POE_C_MU];
+        row[MT_AL] = t[POE_C_ALPHA];
+        row[MT_M] = t[POE_C_RBM];
+        row[MT_RHO] = rho;
+        row[MT_RHOF] = rhof;
+        row[MT_RSM] = rsm;
+        row[MT_EOK] = eok;
+        row[MT_RHOF_EOK] = rhof * eok;
+        row[MT_CO] = co;
+        row[MT_C1] = co + rho * eok * 0.5f;
+        row[MT_C2] = co - rho * eok * 0.5f;
+        row[MT_RCO] = (float)(1.0 / (double)co);
+        row[MT_RC1] = (float)(1.0 / (double)row[MT_C1]);
+        std::memcpy(t, row, sizeof(row));
+        if (!std::isfinite(row[MT_RCO]) || !std::isfinite(row[MT_RC1]) || !std::isnormal(co) ||
+            !std::isnormal(row[MT_C1]))
             return false;   // degenerate material: keep the plane path and IEEE division
     }
     return true;
@@ -423,11 +420,14 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     ModelDev &m = ctx->m;
     m.NX = grid->NX;
     m.NZ = grid->NZ;
-    ctx->ntx = (nx + TILE_X - 1) / TILE_X;
-    ctx->ntz = (nz + TILE_Z - 1) / TILE_Z;
-    // tiles read columns x0-4 .. x0+75 (ids) and rows z0-4 .. z0+35 of their halo
-    m.P = (std::max(ctx->ntx * TILE_X + 16, XH + nx + 4) + 31) / 32 * 32;
-    m.R = ctx->ntz * TILE_Z + 8;
+    // tiles read columns x0-4 .. x0+TX+3 and rows z0-4 .. z0+TZ+3 of their halo;
+    // size the padded planes for both tile shapes (palette 60x32, planes 64x32)
+    {
+        const int px1 = ((nx + TILE_X - 1) / TILE_X) * TILE_X + 8;
+        const int px2 = ((nx + PAL_TX - 1) / PAL_TX) * PAL_TX + 8;
+        m.P = (std::max(std::max(px1, px2), XH + nx + 4) + 31) / 32 * 32;
+        m.R = std::max((nz + TILE_Z - 1) / TILE_Z * TILE_Z, (nz + PAL_TZ - 1) / PAL_TZ * PAL_TZ) + 8;
+    }
     m.plane = (int64_t)m.P * m.R;
     m.dt = grid->dt;
     m.qx = make_div(grid->dx);
@@ -468,11 +468,6 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(ctx->mtab, htab.data(), sizeof(float) * htab.size(), cudaMemcpyHostToDevice,
                                 ctx->stream);
-        CUtensorMap tmi;
-        if (e == cudaSuccess && !encode_ids(&tmi, ctx->ids, m)) e = cudaErrorInvalidValue;
-        if (e == cudaSuccess) e = cudaMalloc(&ctx->tm_ids, sizeof(CUtensorMap));
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(ctx->tm_ids, &tmi, sizeof(CUtensorMap), cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("palette upload: ") + cudaGetErrorString(e));
     } else {
@@ -510,7 +505,11 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     m.ids = ctx->ids;
     m.mtab = ctx->mtab;
     m.nmat = ctx->nmat;
-    m.tm_ids = ctx->tm_ids;
+    // tile geometry of the kernel this model runs on (receiver lists are per tile)
+    ctx->tile_x = ctx->ids ? PAL_TX : TILE_X;
+    ctx->tile_z = ctx->ids ? PAL_TZ : TILE_Z;
+    ctx->ntx = (nx + ctx->tile_x - 1) / ctx->tile_x;
+    ctx->ntz = (nz + ctx->tile_z - 1) / ctx->tile_z;
     *out = ctx;
     return POE_OK;
 }
@@ -541,7 +540,7 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
         if (r.comp == POE_REC_NONE) continue;
         if (r.comp < 0 || r.comp > 2 || r.ix < 0 || r.ix > NX || r.iz < 0 || r.iz > NZ)
             return fail(ctx, POE_EINVAL, "receiver " + std::to_string(i) + " outside the grid");
-        start[(size_t)(r.iz / TILE_Z) * ctx->ntx + r.ix / TILE_X + 1]++;
+        start[(size_t)(r.iz / ctx->tile_z) * ctx->ntx + r.ix / ctx->tile_x + 1]++;
     }
     for (int c = 0; c < ncell; ++c) start[c + 1] += start[c];
     sorted.resize((size_t)start[ncell]);
@@ -550,7 +549,8 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
         for (int i = 0; i < nrec; ++i) {
             const poe_receiver &r = rec[i];
             if (r.comp == POE_REC_NONE) continue;
-            sorted[fill[(size_t)(r.iz / TILE_Z) * ctx->ntx + r.ix / TILE_X]++] = make_int4(r.ix, r.comp, i, r.iz);
+            sorted[fill[(size_t)(r.iz / ctx->tile_z) * ctx->ntx + r.ix / ctx->tile_x]++] =
+                make_int4(r.ix, r.comp, i, r.iz);
         }
     }
     auto bad = [&](cudaError_t e, const char *what) {
@@ -789,7 +789,6 @@ void poe_destroy(poe_ctx *ctx)
     cudaFree(ctx->err_dev);
     cudaFree(ctx->ids);
     cudaFree(ctx->mtab);
-    cudaFree(ctx->tm_ids);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

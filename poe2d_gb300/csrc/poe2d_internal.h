@@ -52,12 +52,17 @@ struct ModelDev {
     const uint8_t *ids;      // padded plane of material ids (pitch P bytes, R rows), or null
     const float *mtab;       // nmat rows of MT_W floats
     int nmat;
-    const void *tm_ids;      // TMA descriptor of the id plane (device memory)
 };
 
-// material-table row: the 8 coefficient planes' values, then quantities the
-// reference derives from them per cell, rounded as it rounds them
-enum { MT_RHOF_EOK = 8, MT_CO, MT_C1, MT_C2, MT_RCO, MT_RC1, MT_W = 16 };
+// material-table row: coefficients and the quantities the reference derives
+// from them per cell, rounded as it rounds them, grouped for 16-byte loads:
+//   [lambda_c mu alpha M] [c2 rhof rho c1] [1/c1 m rhof*eta/kappa co] [1/co eta/kappa - -]
+enum {
+    MT_LC = 0, MT_MU, MT_AL, MT_M,
+    MT_C2, MT_RHOF, MT_RHO, MT_C1,
+    MT_RC1, MT_RSM, MT_RHOF_EOK, MT_CO,
+    MT_RCO, MT_EOK, MT_W = 16
+};
 constexpr int MAX_PALETTE = 64;
 
 // x-strip column of x, or -1
@@ -104,9 +109,11 @@ struct StreamShot {
 
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, int k, bool exact, bool kone,
                      void *stream);
-// TMA box sizes of the palette kernel (elements): velocity tile, stress state, ids
-constexpr int TMA_VW = TILE_X + 8, TMA_VH = TILE_Z + 8, TMA_SH = TILE_Z + 4, TMA_IW = TILE_X + 16,
-              TMA_IH = TILE_Z + 5;
+// palette kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
+// columns = tile + 2-cell halo each side); TMA boxes of 68 x 40 (velocity) and
+// 68 x 36 (stress state) floats
+constexpr int PAL_TX = 60, PAL_TZ = 32;
+constexpr int TMA_VW = PAL_TX + 8, TMA_VH = PAL_TZ + 8, TMA_SH = PAL_TZ + 4;
 int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream);
 // steps[i] += by for every shot
 int launch_advance(int64_t *steps_dev, int nshots, int64_t by, void *stream);

@@ -91,25 +91,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
     return false;
 }
 
-// the descriptor lives in device memory, written by the host before launch
-__device__ __forceinline__ void tma_prefetch_desc(const void *desc)
-{
-    asm volatile("prefetch.tensormap [%0];" ::"l"(desc) : "memory");
-}
-
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0, int c1, int c2, uint64_t *bar)
 {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
         ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0, int c1, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -380,259 +366,336 @@ k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
 // MAX_PALETTE distinct values (patchy models: 2): each cell carries a one-byte
 // material id and every per-cell coefficient the reference computes (co, c1,
 // c2, rhof*eta/kappa, 1/co, 1/c1) comes from a table row in shared memory.
-// All of the tile's inputs (velocity tile + halo, stress state + halo, ids)
-// arrive by TMA in one batch before any computation, so the compute phases
-// read only shared memory.
+//
+// Persistent and double-buffered: one CTA of 512 threads per SM walks the
+// (shot, tile) list.  While it computes tile j from one shared-memory buffer,
+// TMA fills the other with tile j+1 (4 velocity planes + 5 state planes with
+// halos, one batch on an mbarrier) and cp.async brings its material ids, so
+// HBM traffic overlaps compute.  Threads form a 64 x 8 grid: a warp works 32
+// consecutive columns of one row (conflict-free shared-memory access).
 namespace {
-constexpr int PV_FLOATS = TMA_VW * TMA_VH;       // 72 x 40
-constexpr int PS_FLOATS = TMA_VW * TMA_SH;       // 72 x 36
-constexpr int PI_BYTES = TMA_IW * TMA_IH;        // 80 x 37
-constexpr int PAL_OFF_S = 4 * PV_FLOATS * 4;
-constexpr int PAL_OFF_I = PAL_OFF_S + 5 * PS_FLOATS * 4;
-constexpr int PAL_OFF_T = PAL_OFF_I + (PI_BYTES + 127) / 128 * 128;
+constexpr int PNT = 512;
+constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
+constexpr int QSW = QX + 4, QSH = QZ + 4;          // stress cells 64 x 36
+constexpr int IW = TMA_VW, IH = QZ + 5;            // ids: cols x0-4 .. x0+63, rows z0-2 .. z0+34
+constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
+constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
+constexpr int PS_FLOATS = (PS_BOX + 31) / 32 * 32; // slot stride: 128-B aligned TMA destinations
+constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
+constexpr int BUF_OFF_I = BUF_OFF_S + 5 * PS_FLOATS * 4;
+constexpr int BUF_BYTES = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
+constexpr int PAL_OFF_T = 2 * BUF_BYTES;
 constexpr int PAL_OFF_B = PAL_OFF_T + MAX_PALETTE * MT_W * 4;
 constexpr size_t PAL_SMEM = PAL_OFF_B + 16;
-constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_FLOATS * 4 + PI_BYTES;
-static_assert(PAL_OFF_S % 128 == 0 && PAL_OFF_I % 128 == 0 && PAL_OFF_T % 128 == 0, "TMA smem alignment");
+constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4;
+static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
 static_assert((PV_FLOATS * 4) % 128 == 0 && (PS_FLOATS * 4) % 128 == 0, "TMA smem alignment");
+static_assert(IW % 4 == 0 && PAL_SMEM <= 232448, "shared memory budget");
 // state slots in shared memory; after the stress phase they hold its outputs
 enum { PS_G11 = 0, PS_G22, PS_XI1, PS_XI2, PS_SXZ };
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (TMA) writes to the same buffer
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 }  // namespace
 
 template <bool EXACT, bool KONE>
-__global__ void __launch_bounds__(NT, 2)
-k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
+__global__ void __launch_bounds__(PNT, 1)
+k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx, int ntiles, int nitems)
 {
     extern __shared__ __align__(128) unsigned char smp[];
-    float *sv = reinterpret_cast<float *>(smp);                 // 4 x 40 x 72, from (x0-4, z0-4)
-    float *ss = reinterpret_cast<float *>(smp + PAL_OFF_S);     // 5 x 36 x 72, from (x0-4, z0-2)
-    const uint8_t *si = smp + PAL_OFF_I;                         // 37 x 80,     from (x0-4, z0-2)
     float *st = reinterpret_cast<float *>(smp + PAL_OFF_T);     // nmat x MT_W
     uint64_t *bar = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     const int tid = threadIdx.x;
-    const int tx = blockIdx.x % ntx, tz = blockIdx.x / ntx;
-    const StreamShot &S = shots[blockIdx.y];
-    const int64_t n = *S.step + k + 1;
-    const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+    const int lx = tid & 63, ly = tid >> 6;                      // 64 x 8 thread grid
     const int NX = m.NX, NZ = m.NZ;
     const int P = m.P;
     const int64_t PL = m.plane;
-    const int x0 = tx * TX, z0 = tz * TZ;
     const float dt = m.dt;
-    float *__restrict__ FB = S.f[wr];
     const float *__restrict__ PX = m.px;
     const float *__restrict__ PZ = m.pz;
     const int R = m.R;
     const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
-    const int src_off = (int)S.src_off;
-    const int src_where = S.src_where;
-    const bool src_on = n <= S.src_n;
-    const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
 
-    // ---- 1. one batch of TMA loads: 4 velocity planes, 5 state planes, ids
+    // fill buffer b with work item w (thread 0 issues the TMA batch; everyone
+    // issues cp.async for the ids)
+    auto issue = [&](int w, int b) {
+        const int shot = w / ntiles, tile = w - shot * ntiles;
+        const StreamShot &S = shots[shot];
+        const int tx = tile % ntx, tz = tile / ntx;
+        const int x0 = tx * QX, z0 = tz * QZ;
+        unsigned char *buf = smp + b * BUF_BYTES;
+        if (tid == 0) {
+            const int64_t n = *S.step + k + 1;
+            const int cv = (int)((n - 1) & 1) * NSF;
+            float *sv = reinterpret_cast<float *>(buf);
+            float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
+            mbar_expect_tx(&bar[b], PAL_TX_BYTES);
+            for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, &bar[b]);
+            tma_load_3d(ss + PS_G11 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G11, &bar[b]);
+            tma_load_3d(ss + PS_G22 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G22, &bar[b]);
+            tma_load_3d(ss + PS_XI1 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI1, &bar[b]);
+            tma_load_3d(ss + PS_XI2 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI2, &bar[b]);
+            tma_load_3d(ss + PS_SXZ * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_SXZ, &bar[b]);
+        }
+        // ids: rows z0-2 .. z0+34, columns x0-4 .. x0+63 (4-byte aligned: x0 % 4 == 0)
+        const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
+        unsigned char *dst = buf + BUF_OFF_I;
+        for (int i = tid; i < IH * (IW / 4); i += PNT) {
+            const int r = i / (IW / 4), c = i - r * (IW / 4);
+            cp_async4(dst + 4 * i, src + (int64_t)r * P + 4 * c);
+        }
+        cp_async_commit();
+    };
+
     if (tid == 0) {
-        mbar_init(bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         mbar_fence_init();
     }
+    for (int i = tid; i < m.nmat * MT_W; i += PNT) st[i] = m.mtab[i];
     __syncthreads();
-    if (tid == 0) {
-        mbar_expect_tx(bar, PAL_TX_BYTES);
-        const int cv = rd * NSF;
-        for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, bar);
-        const int sp[5] = {SF_G11, SF_G22, SF_XI1, SF_XI2, SF_SXZ};
-        for (int f = 0; f < 5; ++f) tma_load_3d(ss + f * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + sp[f], bar);
-        tma_load_2d(const_cast<uint8_t *>(si), m.tm_ids, x0, z0 + 2, bar);
-    }
-    for (int i = tid; i < m.nmat * MT_W; i += NT) st[i] = m.mtab[i];
-    const float pacc = S.acc[rd];
-    __syncthreads();                                    // table visible
-    if (!mbar_wait(bar, 0)) {                           // bounded: report and leave
-        if (tid == 0) atomicExch(m.err, 1);
-        return;
-    }
+    int w = blockIdx.x;
+    if (w < nitems) issue(w, 0);
 
-    // ---- 2. stress on the tile + 2-cell halo (68 x 36)
-    for (int i = tid; i < S_FLOATS; i += NT) {
-        const int zl = i / SW, xl = i - zl * SW;
-        const int x = x0 - 2 + xl, z = z0 - 2 + zl;
-        const int vo = (zl + 2) * TMA_VW + xl + 2;      // in the velocity tile
-        const int so = zl * TMA_VW + xl + 2;            // in the state tile
-        const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
-        const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
-        const bool cell_ok = x >= 0 && x <= NX && z >= 0 && z <= NZ;
-        const bool g1 = cell_ok && x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;   // cu:60-62
-        const bool g2 = cell_ok && x >= 2 && x <= NX - 1 && z >= 1 && z <= NZ - 2;   // cu:212-214
-        const bool g3 = cell_ok && x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;   // cu:237-239
-        const bool own = cell_ok && x >= x0 && x < x0 + TX && z >= z0 && z < z0 + TZ;
-        const int o = (z + ZH) * P + (x + XH);
-        const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
-        const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
-        const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
-        const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
-        const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
-        const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
-        float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
-        float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
-        float sxz = ss[PS_SXZ * PS_FLOATS + so];
-        const float *mt = st + MT_W * si[zl * TMA_IW + xl + 2];
-        const float *mtop = st + MT_W * si[(zl + 1) * TMA_IW + xl + 2];
-        const float lc = mt[C_LC], mu = mt[C_MU], al = mt[C_AL], M = mt[C_M];
-        const float mu_top = mtop[C_MU];                 // rmu[top] (cu:218)
-        const int xc = cell_ok ? xcol(m, x) : -1;
-        const int zr = cell_ok ? zrow(m, z) : -1;
-        const int xi = x + XH, zi = z + ZH;
-        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-        if (xc >= 0 && (g1 || g2)) {
-            const int ix = z * Wx + xc;
-            const float *MA = S.mx[rd];
+    for (int j = 0; w < nitems; ++j, w += gridDim.x) {
+        const int b = j & 1;
+        const bool ok = mbar_wait(&bar[b], (uint32_t)((j >> 1) & 1));
+        cp_async_wait_all();
+        if (!__syncthreads_and(ok)) {     // a bounded wait gave up: report, drain, leave
+            if (tid == 0) atomicExch(m.err, 1);
+            if (w + (int)gridDim.x < nitems) mbar_wait(&bar[b ^ 1], (uint32_t)(((j + 1) >> 1) & 1));
+            return;
+        }
+        if (w + (int)gridDim.x < nitems) issue(w + gridDim.x, b ^ 1);   // buffer b^1 is free: tile j-1 done
+
+        const int shot = w / ntiles, tile = w - shot * ntiles;
+        const StreamShot &S = shots[shot];
+        const int64_t n = *S.step + k + 1;
+        const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+        const int tx = tile % ntx, tz = tile / ntx;
+        const int x0 = tx * QX, z0 = tz * QZ;
+        float *__restrict__ FB = S.f[wr];
+        const int src_off = (int)S.src_off;
+        const int src_where = S.src_where;
+        const bool src_on = n <= S.src_n;
+        const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
+        const float pacc = S.acc[rd];
+        unsigned char *buf = smp + b * BUF_BYTES;
+        float *sv = reinterpret_cast<float *>(buf);                 // 4 x 40 x 68, from (x0-4, z0-4)
+        float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);     // 5 x 36 x 68, from (x0-4, z0-2)
+        const uint8_t *si = buf + BUF_OFF_I;                         // 37 x 68,     from (x0-4, z0-2)
+
+        // ---- stress on the tile + 2-cell halo: column lx, rows ly, ly+8, ...
+        {
+            const int x = x0 - 2 + lx;
+            const bool x_ok = x >= 0 && x <= NX;
+            const bool x_g1 = x >= 1 && x <= NX - 1, x_g2 = x >= 2 && x <= NX - 1, x_g3 = x >= 1 && x <= NX - 2;
+            const bool x_own = x_ok && lx >= 2 && lx < QX + 2;
+            const int xc = x_ok ? xcol(m, x) : -1;
+            const int xi = x + XH;
             const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-            m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
-            m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
-            m5 = PX[PB * P + xi] * MA[MXS_SXZ * nzx + ix] + PX[PA * P + xi] * sdx;
-            if (own) {
-                float *MB = S.mx[wr];
-                if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
-                if (g2) MB[MXS_SXZ * nzx + ix] = m5;
-            }
-        }
-        if (zr >= 0 && (g1 || g2)) {
-            const int iz = zr * P + xi;
-            const float *MA = S.mz[rd];
-            const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
-            m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
-            m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-            m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
-            if (own) {
-                float *MB = S.mz[wr];
-                if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
-                if (g2) MB[MZS_SXZ * hzp + iz] = m6;
-            }
-        }
-        const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-        const float Kx = KONE ? 1.0f : PX[PK * P + xi];
-        const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
-        if (g1) {   // cu:71-86
-            g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
-            g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
-            xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
-            xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
-        }
-        float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
-        const bool is_src = cell_ok && o == src_off;
-        if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
-        if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-        if (is_src && own) S.acc[wr] = pv;
-        if (g2) {   // cu:223-226
-            const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
-            sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
-        }
-        float sxx = 0.0f, szz = 0.0f;
-        if (g3) {   // cu:241-242
-            if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
-            else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
-        }
-        if (own) {
-            FB[SF_G11 * PL + o] = g11;
-            FB[SF_G22 * PL + o] = g22;
-            FB[SF_XI1 * PL + o] = xi1;
-            FB[SF_XI2 * PL + o] = xi2;
-            FB[SF_SXZ * PL + o] = sxz;
-        }
-        // this thread alone reads these slots of this cell: outputs overwrite inputs
-        ss[PO_SXX * PS_FLOATS + so] = sxx;
-        ss[PO_SZZ * PS_FLOATS + so] = szz;
-        ss[PO_P * PS_FLOATS + so] = pv;
-        ss[PO_SXZ * PS_FLOATS + so] = sxz;
-    }
-    __syncthreads();
-
-    // ---- 3. receivers of this tile (vx, vz before the update; p of this step)
-    if (S.nrec > 0 && n <= S.trace_cap) {
-        const int tile = tz * ntx + tx;
-        const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
-        float *trace_row = S.trace + (n - 1) * S.nrec;
-        for (int q = qb + tid; q < qe; q += NT) {
-            const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
-            const int xl = Rq.x - x0, zl = Rq.w - z0;
-            float v;
-            if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
-            else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
-            trace_row[Rq.z] = v;
-        }
-    }
-
-    // ---- 4. velocity on the tile (64 x 32)
-    float *__restrict__ MXV = S.mxv;
-    float *__restrict__ MZV = S.mzv;
-    for (int i = tid; i < TX * TZ; i += NT) {
-        const int zl = i / TX, xl = i - zl * TX;
-        const int x = x0 + xl, t = z0 + zl;
-        if (x > NX || t > NZ) continue;
-        const int so = (zl + 2) * TMA_VW + xl + 4;      // (x, t) in the stress tile
-        const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
-        const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
-        const int vo = (zl + 4) * TMA_VW + xl + 4;
-        const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
-        const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
-        const int o = (t + ZH) * P + (x + XH);
-        const int xi = x + XH, zi = t + ZH;
-        const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
-        const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
-        const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
-        const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
-        const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
-        const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
-        const bool gvx = x >= 2 && x <= NX - 1 && t >= 2 && t <= NZ - 1;   // cu:289-291
-        const bool gvz = x >= 1 && x <= NX - 2 && t >= 1 && t <= NZ - 2;   // cu:326-328
-        const int xc = xcol(m, x), zr = zrow(m, t);
-        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-        if (xc >= 0 && (gvx || gvz)) {
-            const int ix = t * Wx + xc;
-            float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix, *M4 = MXV + MXV_VZ * nzx + ix;
             const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-            m1 = bx * *M1 + ax * d1x;
-            m2 = bx * *M2 + ax * d2x;
-            m4 = PX[PBH * P + xi] * *M4 + PX[PAH * P + xi] * d1z;
-            if (gvx) { *M1 = m1; *M2 = m2; }
-            if (gvz) *M4 = m4;
+            const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+            const float Kx = KONE ? 1.0f : PX[PK * P + xi];
+            for (int zl = ly; zl < QSH; zl += 8) {
+                const int z = z0 - 2 + zl;
+                const int vo = (zl + 2) * TMA_VW + lx + 2;      // in the velocity tile
+                const int so = zl * TMA_VW + lx + 2;            // in the state tile
+                const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
+                const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
+                const bool z_ok = z >= 0 && z <= NZ;
+                const bool cell_ok = x_ok && z_ok;
+                const bool g1 = cell_ok && x_g1 && z >= 2 && z <= NZ - 2;   // cu:60-62
+                const bool g2 = cell_ok && x_g2 && z >= 1 && z <= NZ - 2;   // cu:212-214
+                const bool g3 = cell_ok && x_g3 && z >= 2 && z <= NZ - 1;   // cu:237-239
+                const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
+                const int o = (z + ZH) * P + xi;
+                const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
+                const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
+                const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
+                const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
+                const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
+                const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
+                float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
+                float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
+                float sxz = ss[PS_SXZ * PS_FLOATS + so];
+                const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * si[zl * IW + lx + 2]);
+                const float mu_top = st[MT_W * si[(zl + 1) * IW + lx + 2] + MT_MU];   // rmu[top] (cu:218)
+                const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
+                const int zr = z_ok ? zrow(m, z) : -1;
+                const int zi = z + ZH;
+                float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+                if (xc >= 0 && (g1 || g2)) {
+                    const int ix = z * Wx + xc;
+                    const float *MA = S.mx[rd];
+                    m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
+                    m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
+                    m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
+                    if (own) {
+                        float *MB = S.mx[wr];
+                        if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
+                        if (g2) MB[MXS_SXZ * nzx + ix] = m5;
+                    }
+                }
+                if (zr >= 0 && (g1 || g2)) {
+                    const int iz = zr * P + xi;
+                    const float *MA = S.mz[rd];
+                    const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
+                    m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
+                    m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
+                    m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
+                    if (own) {
+                        float *MB = S.mz[wr];
+                        if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
+                        if (g2) MB[MZS_SXZ * hzp + iz] = m6;
+                    }
+                }
+                const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
+                if (g1) {   // cu:71-86
+                    g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
+                    g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
+                    xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
+                    xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
+                }
+                float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
+                const bool is_src = cell_ok && o == src_off;
+                if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
+                if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
+                if (is_src && own) S.acc[wr] = pv;
+                if (g2) {   // cu:223-226
+                    const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
+                    sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
+                }
+                float sxx = 0.0f, szz = 0.0f;
+                if (g3) {   // cu:241-242
+                    if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
+                    else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
+                }
+                if (own) {
+                    FB[SF_G11 * PL + o] = g11;
+                    FB[SF_G22 * PL + o] = g22;
+                    FB[SF_XI1 * PL + o] = xi1;
+                    FB[SF_XI2 * PL + o] = xi2;
+                    FB[SF_SXZ * PL + o] = sxz;
+                }
+                // this thread alone reads these slots of this cell: outputs overwrite inputs
+                ss[PO_SXX * PS_FLOATS + so] = sxx;
+                ss[PO_SZZ * PS_FLOATS + so] = szz;
+                ss[PO_P * PS_FLOATS + so] = pv;
+                ss[PO_SXZ * PS_FLOATS + so] = sxz;
+            }
         }
-        if (zr >= 0 && (gvx || gvz)) {
-            const int iz = zr * P + xi;
-            float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz, *M6 = MZV + MZV_VZ2 * hzp + iz;
-            const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
-            m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
-            m5 = bh * *M5 + ah * d2z;
-            m6 = bh * *M6 + ah * d3z;
-            if (gvx) *M3 = m3;
-            if (gvz) { *M5 = m5; *M6 = m6; }
+        __syncthreads();
+
+        // ---- receivers of this tile (vx, vz before the update; p of this step)
+        if (S.nrec > 0 && n <= S.trace_cap) {
+            const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
+            float *trace_row = S.trace + (n - 1) * S.nrec;
+            for (int q = qb + tid; q < qe; q += PNT) {
+                const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
+                const int xl = Rq.x - x0, zl = Rq.w - z0;
+                float v;
+                if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
+                else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
+                trace_row[Rq.z] = v;
+            }
         }
-        const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-        const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
-        float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
-        {   // vx, wx, material at (x, t) (cu:293-311)
-            const float *mt = st + MT_W * si[(zl + 2) * TMA_IW + xl + 4];
-            const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
-            const float B = KDIV<KONE>(d2x, Kx) + m2;
-            const float w1 = div_by(mt[MT_C2] * wx0 + (-mt[C_RHOF] * A - mt[C_RHO] * B), mt[MT_C1], mt[MT_RC1]);
-            const float v1 = vx0 + div_by(mt[C_RSM] * A + mt[C_RHOF] * B + mt[MT_RHOF_EOK] * ((wx0 + w1) * 0.5f),
-                                          mt[MT_CO], mt[MT_RCO]);
-            if (gvx) { wx1 = w1; vx1 = v1; }
+
+        // ---- velocity on the tile: column lx (< 60), rows ly, ly+8, ...
+        if (lx < QX) {
+            float *__restrict__ MXV = S.mxv;
+            float *__restrict__ MZV = S.mzv;
+            const int x = x0 + lx;
+            const bool x_in = x <= NX;
+            const bool x_vx = x >= 2 && x <= NX - 1, x_vz = x >= 1 && x <= NX - 2;   // cu:289, 326
+            const int xc = x_in ? xcol(m, x) : -1;
+            const int xi = x + XH;
+            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
+            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
+            const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+            for (int zl = ly; zl < QZ; zl += 8) {
+                const int t = z0 + zl;
+                if (!x_in || t > NZ) continue;
+                const int so = (zl + 2) * TMA_VW + lx + 4;      // (x, t) in the stress tile
+                const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
+                const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
+                const int vo = (zl + 4) * TMA_VW + lx + 4;
+                const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
+                const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
+                const int o = (t + ZH) * P + xi;
+                const int zi = t + ZH;
+                const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
+                const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
+                const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
+                const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
+                const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
+                const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
+                const bool gvx = x_vx && t >= 2 && t <= NZ - 1;   // cu:289-291
+                const bool gvz = x_vz && t >= 1 && t <= NZ - 2;   // cu:326-328
+                const int zr = zrow(m, t);
+                float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+                if (xc >= 0 && (gvx || gvz)) {
+                    const int ix = t * Wx + xc;
+                    float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
+                    float *M4 = MXV + MXV_VZ * nzx + ix;
+                    m1 = bx * *M1 + ax * d1x;
+                    m2 = bx * *M2 + ax * d2x;
+                    m4 = bxh * *M4 + axh * d1z;
+                    if (gvx) { *M1 = m1; *M2 = m2; }
+                    if (gvz) *M4 = m4;
+                }
+                if (zr >= 0 && (gvx || gvz)) {
+                    const int iz = zr * P + xi;
+                    float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
+                    float *M6 = MZV + MZV_VZ2 * hzp + iz;
+                    const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
+                    m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
+                    m5 = bh * *M5 + ah * d2z;
+                    m6 = bh * *M6 + ah * d3z;
+                    if (gvx) *M3 = m3;
+                    if (gvz) { *M5 = m5; *M6 = m6; }
+                }
+                const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
+                float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
+                {   // vx, wx, material at (x, t) (cu:293-311)
+                    const float *mt = st + MT_W * si[(zl + 2) * IW + lx + 4];
+                    const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
+                    const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
+                    const float rco = mt[MT_RCO];
+                    const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
+                    const float B = KDIV<KONE>(d2x, Kx) + m2;
+                    const float w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                    const float v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
+                    if (gvx) { wx1 = w1; vx1 = v1; }
+                }
+                {   // vz, wz, material at (x, t+1) (cu:330-353)
+                    const float *mt = st + MT_W * si[(zl + 3) * IW + lx + 4];
+                    const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
+                    const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
+                    const float rco = mt[MT_RCO];
+                    float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
+                    const float B = KDIV<KONE>(d3z, Kzh) + m6;
+                    if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
+                    const float w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                    const float v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
+                    if (gvz) { wz1 = w1; vz1 = v1; }
+                }
+                FB[SF_VX * PL + o] = vx1;
+                FB[SF_WX * PL + o] = wx1;
+                FB[SF_VZ * PL + o] = vz1;
+                FB[SF_WZ * PL + o] = wz1;
+            }
         }
-        {   // vz, wz, material at (x, t+1) (cu:330-353)
-            const float *mt = st + MT_W * si[(zl + 3) * TMA_IW + xl + 4];
-            float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
-            const float B = KDIV<KONE>(d3z, Kzh) + m6;
-            if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
-            const float w1 = div_by(mt[MT_C2] * wz0 + (-mt[C_RHOF] * A - mt[C_RHO] * B), mt[MT_C1], mt[MT_RC1]);
-            const float v1 = vz0 + div_by(mt[C_RSM] * A + mt[C_RHOF] * B + mt[MT_RHOF_EOK] * ((wz0 + w1) * 0.5f),
-                                          mt[MT_CO], mt[MT_RCO]);
-            if (gvz) { wz1 = w1; vz1 = v1; }
-        }
-        FB[SF_VX * PL + o] = vx1;
-        FB[SF_WX * PL + o] = wx1;
-        FB[SF_VZ * PL + o] = vz1;
-        FB[SF_WZ * PL + o] = wz1;
+        fence_proxy_async();
+        __syncthreads();   // buffer b is reissued by the next item's prefetch
     }
 }
 
@@ -648,10 +711,21 @@ int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, int k, cud
         cudaFuncSetAttribute(k_tile_pal<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAL_SMEM);
         attr = true;
     }
-    const int ntx = (m.NX + 1 + TX - 1) / TX, ntz = (m.NZ + 1 + TZ - 1) / TZ;
-    dim3 grd(ntx * ntz, nshots);
-    if (m.ids) k_tile_pal<EXACT, KONE><<<grd, NT, PAL_SMEM, st>>>(m, shots, k, ntx);
-    else k_tile<EXACT, KONE><<<grd, NT, TILE_SMEM, st>>>(m, shots, k, ntx);
+    if (m.ids) {
+        const int ntx = (m.NX + 1 + PAL_TX - 1) / PAL_TX, ntz = (m.NZ + 1 + PAL_TZ - 1) / PAL_TZ;
+        const int nitems = ntx * ntz * nshots;
+        static int sms = 0;
+        if (!sms) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        }
+        const int grid = nitems < sms ? nitems : sms;   // persistent: one CTA per SM
+        k_tile_pal<EXACT, KONE><<<grid, PNT, PAL_SMEM, st>>>(m, shots, k, ntx, ntx * ntz, nitems);
+    } else {
+        const int ntx = (m.NX + 1 + TX - 1) / TX, ntz = (m.NZ + 1 + TZ - 1) / TZ;
+        k_tile<EXACT, KONE><<<dim3(ntx * ntz, nshots), NT, TILE_SMEM, st>>>(m, shots, k, ntx);
+    }
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -691,7 +765,11 @@ __global__ void k_derive(const ModelDev m, const StreamShot *__restrict__ shots,
     const int64_t P = m.P, PL = m.plane;
     const int64_t o = (int64_t)(z + ZH) * P + (x + XH);
     const float *F = S.f[n & 1];
-    auto coef = [&](int c) { return m.ids ? m.mtab[MT_W * m.ids[o] + c] : m.coef[c * PL + o]; };
+    // coefficient c (plane order) from the planes or the palette table
+    auto coef = [&](int c) {
+        const int mt = c == C_LC ? MT_LC : (c == C_MU ? MT_MU : (c == C_AL ? MT_AL : MT_M));
+        return m.ids ? m.mtab[MT_W * m.ids[o] + mt] : m.coef[c * PL + o];
+    };
     const bool g1 = x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;
     const bool g3 = x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;
     const float g11 = F[SF_G11 * PL + o], g22 = F[SF_G22 * PL + o];
