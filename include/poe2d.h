@@ -187,6 +187,20 @@ int poe_get_traces(poe_ctx *ctx, int32_t shot, float *host_out, int64_t capacity
 /* One full field of a shot, (NX+1)*(NZ+1) floats, x fastest (cu:1642-1645). */
 int poe_get_field(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out);
 
+/* sigma_xx, sigma_zz or p (POE_F_SXX / POE_F_SZZ / POE_F_P) of a shot, like
+ * poe_get_field, but allocating nothing: no reference counterpart.  For callers
+ * that cannot allocate device memory (a fixed memory budget, a pool shared with
+ * other work, or code between allocation-free phases): poe_get_field builds
+ * these fields in a device buffer it allocates on first use, this entry point
+ * builds them in a static 32 MiB plane that every GPU loading the library
+ * holds until the process exits.  Limit: padded planes of at most 8 Mi floats
+ * (grids up to about 2850 x 2850); larger ones return POE_EINVAL.  The first
+ * call on a device looks up that plane's device address, so make it before any
+ * stream capture.  All calls share the plane: calls that overlap on the GPU
+ * (several contexts or threads at once) race, so serialise them.  Every cell
+ * read back is written by the same call, nothing needs clearing. */
+int poe_get_derived_noalloc(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out);
+
 /* Overwrite one full field of a shot (checkpoint restore; no reference counterpart). */
 int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in);
 

@@ -76,6 +76,7 @@ SYMBOLS = {
     "poe_get_traces": (C.c_int, [C.c_void_p, C.c_int32, _fp, C.c_int64]),
     "poe_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
+    "poe_get_derived_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_reset_shot": (C.c_int, [C.c_void_p, C.c_int32]),
     "poe_check_finite": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, _fp]),

@@ -697,6 +697,26 @@ int poe_get_field(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out)
     return device_status(ctx);
 }
 
+int poe_get_derived_noalloc(poe_ctx *ctx, int32_t shot, int32_t field, float *host_out)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    if (!host_out) return fail(ctx, POE_EINVAL, "null output");
+    if (field != POE_F_SXX && field != POE_F_SZZ && field != POE_F_P)
+        return fail(ctx, POE_EINVAL, "only sigma_xx, sigma_zz and p are derived; read the others with poe_get_field");
+    const ModelDev &m = ctx->m;
+    if (m.plane > NOALLOC_SCRATCH_FLOATS)
+        return fail(ctx, POE_EINVAL,
+                    "padded plane of " + std::to_string(m.plane) + " floats exceeds the static scratch of " +
+                        std::to_string(NOALLOC_SCRATCH_FLOATS) + " floats");
+    CK(cudaSetDevice(ctx->device));
+    const int which = field == POE_F_SXX ? 0 : (field == POE_F_SZZ ? 1 : 2);
+    const int rc = derive_noalloc(m, s->f[s->steps & 1], s->acc, s->src_off, s->src_where, s->src_n, s->src_tab,
+                                  s->steps, which, host_out, ctx->stream);
+    if (rc != 0) return fail(ctx, POE_ECUDA, std::string("derived read-out: ") + cudaGetErrorString((cudaError_t)rc));
+    return device_status(ctx);
+}
+
 int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in)
 {
     ShotHost *s = get_shot(ctx, shot);

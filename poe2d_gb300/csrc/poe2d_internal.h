@@ -115,6 +115,11 @@ int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots,
 constexpr int PAL_TX = 60, PAL_TZ = 32;
 constexpr int TMA_VW = PAL_TX + 8, TMA_VH = PAL_TZ + 8, TMA_SH = PAL_TZ + 4;
 int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream);
+// allocation-free read-out of one derived field (sigma_xx 0, sigma_zz 1, p 2)
+// through the library's static scratch plane; returns a cudaError_t
+constexpr int64_t NOALLOC_SCRATCH_FLOATS = (int64_t)8 << 20;
+int derive_noalloc(const ModelDev &m, const float *F, const float *acc, int64_t src_off, int src_where,
+                   int64_t src_n, const float *src_tab, int64_t n, int which, float *host_out, void *stream);
 // steps[i] += by for every shot
 int launch_advance(int64_t *steps_dev, int nshots, int64_t by, void *stream);
 

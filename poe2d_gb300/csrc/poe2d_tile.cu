@@ -20,6 +20,8 @@
 // stencils (FAST); compiled with -fmad=false.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "poe2d_internal.h"
 
 namespace poe {
@@ -793,6 +795,82 @@ int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int6
     dim3 grd((m.NX + 1 + 127) / 128, m.NZ + 1);
     k_derive<<<grd, 128, 0, (cudaStream_t)stream>>>(m, shots_dev, shot, n, out);
     return (int)cudaGetLastError();
+}
+
+// ---- allocation-free read-out of one derived field ----
+// For callers that cannot allocate device memory: the one-plane scratch lives
+// in this file-scope array, loaded with the library and held by every device
+// that loads it until the process exits.  32 MiB: padded planes of up to
+// 8 Mi floats (grids up to about 2850 x 2850 cells).
+static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_SCRATCH_FLOATS];
+
+// sigma_xx (which = 0), sigma_zz (1) or p (2) of one shot's current state into
+// one padded plane; the same arithmetic as k_derive
+__global__ void k_derive_one(const ModelDev m, const float *__restrict__ F, const float *__restrict__ acc,
+                             int64_t src_off, int src_where, int64_t src_n, const float *__restrict__ src_tab,
+                             int64_t n, int which, float *out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = blockIdx.y;
+    if (x > m.NX || z > m.NZ) return;
+    const int NX = m.NX, NZ = m.NZ;
+    const int64_t P = m.P, PL = m.plane;
+    const int64_t o = (int64_t)(z + ZH) * P + (x + XH);
+    auto coef = [&](int c) {
+        const int mt = c == C_LC ? MT_LC : (c == C_MU ? MT_MU : (c == C_AL ? MT_AL : MT_M));
+        return m.ids ? m.mtab[MT_W * m.ids[o] + mt] : m.coef[c * PL + o];
+    };
+    const bool g1 = x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;
+    const bool g3 = x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;
+    const float g11 = F[SF_G11 * PL + o], g22 = F[SF_G22 * PL + o];
+    const float al = coef(C_AL), M = coef(C_M);
+    float pv = 0.0f;
+    if (g1) pv = -al * M * (g11 + g22) + M * (F[SF_XI1 * PL + o] + F[SF_XI2 * PL + o]);
+    if (o == src_off) {
+        if (!g1) pv = acc[n & 1];
+        else if (src_where == SRC_P && n >= 1 && n <= src_n) pv = pv + src_tab[n - 1];
+    }
+    float sxx = 0.0f, szz = 0.0f;
+    if (g3) sxx_szz_exact(coef(C_LC), coef(C_MU), g11, g22, al, pv, sxx, szz);
+    out[o] = which == 0 ? sxx : (which == 1 ? szz : pv);
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+float *g_noalloc_ptr[256] = {};   // device address of g_noalloc_scratch, per device ordinal
+}  // namespace
+
+int derive_noalloc(const ModelDev &m, const float *F, const float *acc, int64_t src_off, int src_where,
+                   int64_t src_n, const float *src_tab, int64_t n, int which, float *host_out, void *stream)
+{
+    if (m.plane > NOALLOC_SCRATCH_FLOATS) return (int)cudaErrorInvalidValue;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= 256) return (int)cudaErrorInvalidDevice;
+    float *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            // the array's name is a host-side stand-in: its device address is
+            // looked up once per device, with that device current
+            e = cudaGetSymbolAddress((void **)&g_noalloc_ptr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                return (int)e;
+            }
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grd((m.NX + 1 + 127) / 128, m.NZ + 1);
+    k_derive_one<<<grd, 128, 0, st>>>(m, F, acc, src_off, src_where, src_n, src_tab, n, which, scratch);
+    if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+    const int nx = m.NX + 1, nz = m.NZ + 1;
+    e = cudaMemcpy2DAsync(host_out, sizeof(float) * nx, scratch + (int64_t)ZH * m.P + XH, sizeof(float) * m.P,
+                          sizeof(float) * nx, nz, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaStreamSynchronize(st);
 }
 
 }  // namespace poe

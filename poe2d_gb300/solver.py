@@ -185,6 +185,13 @@ class Solver:
         self._check(L.lib().poe_get_field(self.h, shot, fid, _f(out)))
         return out
 
+    def derived_noalloc(self, name, shot=0):
+        """sigma_xx, sigma_zz or p without any device allocation (static scratch plane)."""
+        fid = L.FIELDS.index(name) if isinstance(name, str) else int(name)
+        out = np.empty(self.shape, np.float32)
+        self._check(L.lib().poe_get_derived_noalloc(self.h, shot, fid, _f(out)))
+        return out
+
     def set_field(self, name, values, shot=0):
         fid = L.FIELDS.index(name) if isinstance(name, str) else int(name)
         a = np.ascontiguousarray(np.asarray(values, np.float32).reshape(self.shape))
