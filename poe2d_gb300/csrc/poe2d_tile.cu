@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "poe2d_internal.h"
 
@@ -40,6 +41,14 @@ constexpr int NT = 256;
 #endif
 constexpr int kStressUnroll = STRESS_UNROLL;   // cells in flight per thread (memory-level parallelism)
 constexpr int kVelUnroll = VEL_UNROLL;
+#ifndef PAL_SUNROLL
+#define PAL_SUNROLL 1
+#endif
+#ifndef PAL_VUNROLL
+#define PAL_VUNROLL 1
+#endif
+constexpr int kPalStressUnroll = PAL_SUNROLL;   // palette kernel: rows per thread interleaved
+constexpr int kPalVelUnroll = PAL_VUNROLL;
 constexpr int V_FLOATS = VW * VH, S_FLOATS = SW * SH;
 enum { SV_VX = 0, SV_VZ, SV_WX, SV_WZ };
 enum { SS_SXX = 0, SS_SZZ, SS_SXZ, SS_P };
@@ -495,206 +504,223 @@ k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int nt
         float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);     // 5 x 36 x 68, from (x0-4, z0-2)
         const uint8_t *si = buf + BUF_OFF_I;                         // 37 x 68,     from (x0-4, z0-2)
 
-        // ---- stress on the tile + 2-cell halo: column lx, rows ly, ly+8, ...
+        // Interior tiles (no grid edge, C-PML strip or source within the tile
+        // and its halo) take a copy of the code with every guard constant-true.
+        auto compute = [&](auto interior_tag) {
+            constexpr bool IN = decltype(interior_tag)::value;
+            // ---- stress on the tile + 2-cell halo: column lx, rows ly, ly+8, ...
+            {
+                const int x = x0 - 2 + lx;
+                const bool x_ok = IN || (x >= 0 && x <= NX);
+                const bool x_g1 = IN || (x >= 1 && x <= NX - 1), x_g2 = IN || (x >= 2 && x <= NX - 1);
+                const bool x_g3 = IN || (x >= 1 && x <= NX - 2);
+                const bool x_own = x_ok && lx >= 2 && lx < QX + 2;
+                const int xc = (!IN && x_ok) ? xcol(m, x) : -1;
+                const int xi = x + XH;
+                const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
+                const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
+                const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+                const float Kx = KONE ? 1.0f : PX[PK * P + xi];
+#pragma unroll kPalStressUnroll
+                for (int zl = ly; zl < QSH; zl += 8) {
+                    const int z = z0 - 2 + zl;
+                    const int vo = (zl + 2) * TMA_VW + lx + 2;      // in the velocity tile
+                    const int so = zl * TMA_VW + lx + 2;            // in the state tile
+                    const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
+                    const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
+                    const bool z_ok = IN || (z >= 0 && z <= NZ);
+                    const bool cell_ok = x_ok && z_ok;
+                    const bool g1 = IN || (cell_ok && x_g1 && z >= 2 && z <= NZ - 2);   // cu:60-62
+                    const bool g2 = IN || (cell_ok && x_g2 && z >= 1 && z <= NZ - 2);   // cu:212-214
+                    const bool g3 = IN || (cell_ok && x_g3 && z >= 2 && z <= NZ - 1);   // cu:237-239
+                    const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
+                    const int o = (z + ZH) * P + xi;
+                    const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
+                    const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
+                    const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
+                    const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
+                    const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
+                    const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
+                    float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
+                    float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
+                    float sxz = ss[PS_SXZ * PS_FLOATS + so];
+                    const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * si[zl * IW + lx + 2]);
+                    const float mu_top = st[MT_W * si[(zl + 1) * IW + lx + 2] + MT_MU];   // rmu[top] (cu:218)
+                    const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
+                    const int zr = (!IN && z_ok) ? zrow(m, z) : -1;
+                    const int zi = z + ZH;
+                    float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+                    if (xc >= 0 && (g1 || g2)) {
+                        const int ix = z * Wx + xc;
+                        const float *MA = S.mx[rd];
+                        m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
+                        m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
+                        m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
+                        if (own) {
+                            float *MB = S.mx[wr];
+                            if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
+                            if (g2) MB[MXS_SXZ * nzx + ix] = m5;
+                        }
+                    }
+                    if (zr >= 0 && (g1 || g2)) {
+                        const int iz = zr * P + xi;
+                        const float *MA = S.mz[rd];
+                        const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
+                        m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
+                        m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
+                        m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
+                        if (own) {
+                            float *MB = S.mz[wr];
+                            if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
+                            if (g2) MB[MZS_SXZ * hzp + iz] = m6;
+                        }
+                    }
+                    const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
+                    if (g1) {   // cu:71-86
+                        g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
+                        g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
+                        xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
+                        xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
+                    }
+                    float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
+                    const bool is_src = !IN && cell_ok && o == src_off;
+                    if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
+                    if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
+                    if (is_src && own) S.acc[wr] = pv;
+                    if (g2) {   // cu:223-226
+                        const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
+                        sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
+                    }
+                    float sxx = 0.0f, szz = 0.0f;
+                    if (g3) {   // cu:241-242
+                        if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
+                        else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
+                    }
+                    if (own) {
+                        FB[SF_G11 * PL + o] = g11;
+                        FB[SF_G22 * PL + o] = g22;
+                        FB[SF_XI1 * PL + o] = xi1;
+                        FB[SF_XI2 * PL + o] = xi2;
+                        FB[SF_SXZ * PL + o] = sxz;
+                    }
+                    // this thread alone reads these slots of this cell: outputs overwrite inputs
+                    ss[PO_SXX * PS_FLOATS + so] = sxx;
+                    ss[PO_SZZ * PS_FLOATS + so] = szz;
+                    ss[PO_P * PS_FLOATS + so] = pv;
+                    ss[PO_SXZ * PS_FLOATS + so] = sxz;
+                }
+            }
+            __syncthreads();
+
+            // ---- receivers of this tile (vx, vz before the update; p of this step)
+            if (S.nrec > 0 && n <= S.trace_cap) {
+                const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
+                float *trace_row = S.trace + (n - 1) * S.nrec;
+                for (int q = qb + tid; q < qe; q += PNT) {
+                    const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
+                    const int xl = Rq.x - x0, zl = Rq.w - z0;
+                    float v;
+                    if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
+                    else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
+                    trace_row[Rq.z] = v;
+                }
+            }
+
+            // ---- velocity on the tile: column lx (< 60), rows ly, ly+8, ...
+            if (lx < QX) {
+                float *__restrict__ MXV = S.mxv;
+                float *__restrict__ MZV = S.mzv;
+                const int x = x0 + lx;
+                const bool x_in = IN || x <= NX;
+                const bool x_vx = IN || (x >= 2 && x <= NX - 1), x_vz = IN || (x >= 1 && x <= NX - 2);   // cu:289, 326
+                const int xc = (!IN && x_in) ? xcol(m, x) : -1;
+                const int xi = x + XH;
+                const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
+                const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
+                const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+#pragma unroll kPalVelUnroll
+                for (int zl = ly; zl < QZ; zl += 8) {
+                    const int t = z0 + zl;
+                    if (!IN && (!x_in || t > NZ)) continue;
+                    const int so = (zl + 2) * TMA_VW + lx + 4;      // (x, t) in the stress tile
+                    const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
+                    const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
+                    const int vo = (zl + 4) * TMA_VW + lx + 4;
+                    const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
+                    const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
+                    const int o = (t + ZH) * P + xi;
+                    const int zi = t + ZH;
+                    const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
+                    const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
+                    const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
+                    const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
+                    const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
+                    const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
+                    const bool gvx = IN || (x_vx && t >= 2 && t <= NZ - 1);   // cu:289-291
+                    const bool gvz = IN || (x_vz && t >= 1 && t <= NZ - 2);   // cu:326-328
+                    const int zr = IN ? -1 : zrow(m, t);
+                    float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
+                    if (xc >= 0 && (gvx || gvz)) {
+                        const int ix = t * Wx + xc;
+                        float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
+                        float *M4 = MXV + MXV_VZ * nzx + ix;
+                        m1 = bx * *M1 + ax * d1x;
+                        m2 = bx * *M2 + ax * d2x;
+                        m4 = bxh * *M4 + axh * d1z;
+                        if (gvx) { *M1 = m1; *M2 = m2; }
+                        if (gvz) *M4 = m4;
+                    }
+                    if (zr >= 0 && (gvx || gvz)) {
+                        const int iz = zr * P + xi;
+                        float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
+                        float *M6 = MZV + MZV_VZ2 * hzp + iz;
+                        const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
+                        m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
+                        m5 = bh * *M5 + ah * d2z;
+                        m6 = bh * *M6 + ah * d3z;
+                        if (gvx) *M3 = m3;
+                        if (gvz) { *M5 = m5; *M6 = m6; }
+                    }
+                    const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
+                    float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
+                    {   // vx, wx, material at (x, t) (cu:293-311)
+                        const float *mt = st + MT_W * si[(zl + 2) * IW + lx + 4];
+                        const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
+                        const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
+                        const float rco = mt[MT_RCO];
+                        const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
+                        const float B = KDIV<KONE>(d2x, Kx) + m2;
+                        const float w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                        const float v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
+                        if (gvx) { wx1 = w1; vx1 = v1; }
+                    }
+                    {   // vz, wz, material at (x, t+1) (cu:330-353)
+                        const float *mt = st + MT_W * si[(zl + 3) * IW + lx + 4];
+                        const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
+                        const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
+                        const float rco = mt[MT_RCO];
+                        float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
+                        const float B = KDIV<KONE>(d3z, Kzh) + m6;
+                        if (!IN && o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
+                        const float w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                        const float v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
+                        if (gvz) { wz1 = w1; vz1 = v1; }
+                    }
+                    FB[SF_VX * PL + o] = vx1;
+                    FB[SF_WX * PL + o] = wx1;
+                    FB[SF_VZ * PL + o] = vz1;
+                    FB[SF_WZ * PL + o] = wz1;
+                }
+            }
+        };
         {
-            const int x = x0 - 2 + lx;
-            const bool x_ok = x >= 0 && x <= NX;
-            const bool x_g1 = x >= 1 && x <= NX - 1, x_g2 = x >= 2 && x <= NX - 1, x_g3 = x >= 1 && x <= NX - 2;
-            const bool x_own = x_ok && lx >= 2 && lx < QX + 2;
-            const int xc = x_ok ? xcol(m, x) : -1;
-            const int xi = x + XH;
-            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-            const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-            const float Kx = KONE ? 1.0f : PX[PK * P + xi];
-            for (int zl = ly; zl < QSH; zl += 8) {
-                const int z = z0 - 2 + zl;
-                const int vo = (zl + 2) * TMA_VW + lx + 2;      // in the velocity tile
-                const int so = zl * TMA_VW + lx + 2;            // in the state tile
-                const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
-                const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
-                const bool z_ok = z >= 0 && z <= NZ;
-                const bool cell_ok = x_ok && z_ok;
-                const bool g1 = cell_ok && x_g1 && z >= 2 && z <= NZ - 2;   // cu:60-62
-                const bool g2 = cell_ok && x_g2 && z >= 1 && z <= NZ - 2;   // cu:212-214
-                const bool g3 = cell_ok && x_g3 && z >= 2 && z <= NZ - 1;   // cu:237-239
-                const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
-                const int o = (z + ZH) * P + xi;
-                const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
-                const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
-                const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
-                const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
-                const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
-                const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
-                float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
-                float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
-                float sxz = ss[PS_SXZ * PS_FLOATS + so];
-                const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * si[zl * IW + lx + 2]);
-                const float mu_top = st[MT_W * si[(zl + 1) * IW + lx + 2] + MT_MU];   // rmu[top] (cu:218)
-                const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
-                const int zr = z_ok ? zrow(m, z) : -1;
-                const int zi = z + ZH;
-                float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-                if (xc >= 0 && (g1 || g2)) {
-                    const int ix = z * Wx + xc;
-                    const float *MA = S.mx[rd];
-                    m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
-                    m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
-                    m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
-                    if (own) {
-                        float *MB = S.mx[wr];
-                        if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
-                        if (g2) MB[MXS_SXZ * nzx + ix] = m5;
-                    }
-                }
-                if (zr >= 0 && (g1 || g2)) {
-                    const int iz = zr * P + xi;
-                    const float *MA = S.mz[rd];
-                    const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
-                    m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
-                    m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-                    m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
-                    if (own) {
-                        float *MB = S.mz[wr];
-                        if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
-                        if (g2) MB[MZS_SXZ * hzp + iz] = m6;
-                    }
-                }
-                const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
-                if (g1) {   // cu:71-86
-                    g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
-                    g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
-                    xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
-                    xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
-                }
-                float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
-                const bool is_src = cell_ok && o == src_off;
-                if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
-                if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-                if (is_src && own) S.acc[wr] = pv;
-                if (g2) {   // cu:223-226
-                    const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
-                    sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
-                }
-                float sxx = 0.0f, szz = 0.0f;
-                if (g3) {   // cu:241-242
-                    if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
-                    else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
-                }
-                if (own) {
-                    FB[SF_G11 * PL + o] = g11;
-                    FB[SF_G22 * PL + o] = g22;
-                    FB[SF_XI1 * PL + o] = xi1;
-                    FB[SF_XI2 * PL + o] = xi2;
-                    FB[SF_SXZ * PL + o] = sxz;
-                }
-                // this thread alone reads these slots of this cell: outputs overwrite inputs
-                ss[PO_SXX * PS_FLOATS + so] = sxx;
-                ss[PO_SZZ * PS_FLOATS + so] = szz;
-                ss[PO_P * PS_FLOATS + so] = pv;
-                ss[PO_SXZ * PS_FLOATS + so] = sxz;
-            }
-        }
-        __syncthreads();
-
-        // ---- receivers of this tile (vx, vz before the update; p of this step)
-        if (S.nrec > 0 && n <= S.trace_cap) {
-            const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
-            float *trace_row = S.trace + (n - 1) * S.nrec;
-            for (int q = qb + tid; q < qe; q += PNT) {
-                const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
-                const int xl = Rq.x - x0, zl = Rq.w - z0;
-                float v;
-                if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
-                else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
-                trace_row[Rq.z] = v;
-            }
-        }
-
-        // ---- velocity on the tile: column lx (< 60), rows ly, ly+8, ...
-        if (lx < QX) {
-            float *__restrict__ MXV = S.mxv;
-            float *__restrict__ MZV = S.mzv;
-            const int x = x0 + lx;
-            const bool x_in = x <= NX;
-            const bool x_vx = x >= 2 && x <= NX - 1, x_vz = x >= 1 && x <= NX - 2;   // cu:289, 326
-            const int xc = x_in ? xcol(m, x) : -1;
-            const int xi = x + XH;
-            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-            const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-            for (int zl = ly; zl < QZ; zl += 8) {
-                const int t = z0 + zl;
-                if (!x_in || t > NZ) continue;
-                const int so = (zl + 2) * TMA_VW + lx + 4;      // (x, t) in the stress tile
-                const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
-                const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
-                const int vo = (zl + 4) * TMA_VW + lx + 4;
-                const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
-                const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
-                const int o = (t + ZH) * P + xi;
-                const int zi = t + ZH;
-                const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
-                const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
-                const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
-                const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
-                const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
-                const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
-                const bool gvx = x_vx && t >= 2 && t <= NZ - 1;   // cu:289-291
-                const bool gvz = x_vz && t >= 1 && t <= NZ - 2;   // cu:326-328
-                const int zr = zrow(m, t);
-                float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-                if (xc >= 0 && (gvx || gvz)) {
-                    const int ix = t * Wx + xc;
-                    float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
-                    float *M4 = MXV + MXV_VZ * nzx + ix;
-                    m1 = bx * *M1 + ax * d1x;
-                    m2 = bx * *M2 + ax * d2x;
-                    m4 = bxh * *M4 + axh * d1z;
-                    if (gvx) { *M1 = m1; *M2 = m2; }
-                    if (gvz) *M4 = m4;
-                }
-                if (zr >= 0 && (gvx || gvz)) {
-                    const int iz = zr * P + xi;
-                    float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
-                    float *M6 = MZV + MZV_VZ2 * hzp + iz;
-                    const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
-                    m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
-                    m5 = bh * *M5 + ah * d2z;
-                    m6 = bh * *M6 + ah * d3z;
-                    if (gvx) *M3 = m3;
-                    if (gvz) { *M5 = m5; *M6 = m6; }
-                }
-                const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
-                float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
-                {   // vx, wx, material at (x, t) (cu:293-311)
-                    const float *mt = st + MT_W * si[(zl + 2) * IW + lx + 4];
-                    const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
-                    const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
-                    const float rco = mt[MT_RCO];
-                    const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
-                    const float B = KDIV<KONE>(d2x, Kx) + m2;
-                    const float w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                    const float v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
-                    if (gvx) { wx1 = w1; vx1 = v1; }
-                }
-                {   // vz, wz, material at (x, t+1) (cu:330-353)
-                    const float *mt = st + MT_W * si[(zl + 3) * IW + lx + 4];
-                    const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
-                    const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
-                    const float rco = mt[MT_RCO];
-                    float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
-                    const float B = KDIV<KONE>(d3z, Kzh) + m6;
-                    if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
-                    const float w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                    const float v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
-                    if (gvz) { wz1 = w1; vz1 = v1; }
-                }
-                FB[SF_VX * PL + o] = vx1;
-                FB[SF_WX * PL + o] = wx1;
-                FB[SF_VZ * PL + o] = vz1;
-                FB[SF_WZ * PL + o] = wz1;
-            }
+            int sx = -1000000, sz = -1000000;
+            if (src_off >= 0) { sz = src_off / P - ZH; sx = src_off - (sz + ZH) * P - XH; }
+            const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
+            const bool interior = xa >= 2 && xa >= m.xL && xb <= NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
+                                  zb <= NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
+            if (interior) compute(std::true_type{});
+            else compute(std::false_type{});
         }
         fence_proxy_async();
         __syncthreads();   // buffer b is reissued by the next item's prefetch

@@ -134,11 +134,13 @@ def test_palette_path_matches_planes_and_oracle(poe, oracle_mod, fast):
     cell, TMA-staged tiles); the same model with palette=False runs on the
     coefficient-plane kernel.  Both must agree bit for bit, and with the oracle."""
     O = oracle_mod
-    NX, NZ, dx, dt, f0, n = 130, 97, 0.5, 5e-5, 200.0, 140
+    # 251 x 201 with a 10-cell C-PML: most 60 x 32 tiles are interior (no
+    # edge, strip or source), the rest take the guarded path
+    NX, NZ, dx, dt, f0, n = 250, 200, 0.5, 5e-5, 200.0, 140
     coef, vp = _patchy(poe, NX, NZ, 5)
     g = poe.grid(NX, NZ, dx, dt)
-    px, pz = poe.pml_profiles(g, 12, f0, vp)
-    rec = [(x, 15, c) for c in (0, 1, 2) for x in range(14, 120, 13)]
+    px, pz = poe.pml_profiles(g, 10, f0, vp)
+    rec = [(x, 15, c) for c in (0, 1, 2) for x in range(14, 240, 19)] + [(130, 100, 2), (95, 150, 1)]
     src = poe.source(64, 50, poe.SRC_RICKER_FZ, f0, 1e3, 0.0)
     out = {}
     for pal in (True, False):
