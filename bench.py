@@ -67,6 +67,124 @@ def workload(seed=0, shift=0):
     return g, coef, px, pz, src, rec, ids
 
 
+def shots_model(nshots=64, n=1001, npml=30, nrec=256):
+    """The batched-shots workload: one n x n patchy model (the statistics of
+    the single-shot model, 30-cell C-PML), nshots Ricker sources spaced evenly
+    along the surface row, nrec surface receivers x (vx, vz, p) per shot."""
+    import poe2d_gb300 as P
+    from poe2d_gb300.patchy import random_patches
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = P.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    gas = P.biot_material(rho_f=100.0, k_f=0.02e9, eta=1e-5, **frame)
+    ids = random_patches((n, n), DX, fraction=0.10, r_min=2.0, r_max=10.0, seed=4321)
+    coef, vp = P.coeffs_biot([water, gas], ids)
+    g = P.grid(n - 1, n - 1, DX, DT)
+    P.check_courant(g, vp)
+    px, pz = P.pml_profiles(g, npml, F0, vp)
+    span = n - 1 - 2 * npml - 2
+    srcs = [P.source(int(npml + 1 + (k * span) // max(nshots - 1, 1)), npml, P.SRC_RICKER_FZ, F0, 1e6, 0.0)
+            for k in range(nshots)]
+    xs = npml + 1 + (np.arange(nrec) * span) // (nrec - 1)
+    rec = [(int(x), npml, c) for c in (P.REC_VX, P.REC_VZ, P.REC_P) for x in xs]
+    return g, coef, px, pz, srcs, rec
+
+
+def timed(stream, fn):
+    """CUDA-event time (s) of fn() on stream, synchronised on both sides."""
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def leg_shots(P, stream, fast, nsteps=10000, nshots=64, single_shots=2):
+    """64 shots of one model advanced together (one persistent launch per
+    time step over every tile of every shot) against the same shots run one at
+    a time; the batched traces of shot 0 must equal its single run's bit for bit."""
+    g, coef, px, pz, srcs, rec = shots_model(nshots)
+    cells = (g.NX + 1) * (g.NZ + 1)
+    sb = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=fast)
+    for s in srcs:
+        sb.add_shot(s, rec)
+    sb.run(64)                                   # warm-up: graph capture, first touch
+    for k in range(nshots):
+        sb.reset_shot(k)
+    t_b = timed(stream, lambda: sb.run(nsteps))
+    tr_b = sb.traces(0)
+    sb.close()
+    s1 = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=fast)
+    s1.add_shot(srcs[0], rec)
+    s1.run(64)
+    s1.reset_shot(0)
+
+    def singles():
+        for _ in range(single_shots):
+            s1.reset_shot(0)
+            s1.run(nsteps)
+    t_1 = timed(stream, singles) / single_shots
+    same = bool(np.array_equal(s1.traces(0).view(np.uint32), tr_b.view(np.uint32)))
+    s1.close()
+    vb = cells * nsteps * nshots / t_b / 1e9
+    v1 = cells * nsteps / t_1 / 1e9
+    return {"workload": "%d shots x %dx%d patchy model, 30-cell C-PML, %d steps, %d receivers x (vx,vz,p) per shot"
+                        % (nshots, g.NX + 1, g.NZ + 1, nsteps, len(rec) // 3),
+            "batched_gcells": vb, "single_shot_gcells": v1, "speedup_vs_1shot": vb / v1,
+            "batched_s": t_b, "single_shot_s": t_1,
+            "single_shot_sample": "%d single-shot runs back to back, mean" % single_shots,
+            "shot0_bitwise_equal_to_single_run": same}
+
+
+def leg_uneven(P, stream, fast, nmodels, seed=7):
+    """The uneven batch: nmodels independent patchy realisations, side
+    U[256, 1536], steps 4 x side, one centre-surface shot each with 128
+    receivers x (vx, vz, p); one batch against back-to-back single runs."""
+    from poe2d_gb300 import datagen as D
+    specs = D.uneven_specs(seed, 256)[:nmodels]
+    t0 = time.perf_counter()
+    solvers, steps = [], []
+    work = 0
+    for sp in specs:
+        g, coef, px, pz, src, rec, ids = D.build_model(sp)
+        s = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=fast)
+        s.add_shot(src, rec)
+        solvers.append(s)
+        steps.append(sp["steps"])
+        work += (g.NX + 1) * (g.NZ + 1) * sp["steps"]
+    setup = time.perf_counter() - t0
+    batch = P.Batch(solvers, stream=stream.cuda_stream)
+    batch.run([64] * len(solvers))               # warm-up: graph capture, first touch
+    for s in solvers:
+        s.reset_shot(0)
+    l0 = batch.launches
+    t_b = timed(stream, lambda: batch.run(steps))
+    launches = batch.launches - l0
+    batch.sync()
+    tr_b = [s.traces(0) for s in solvers[:4]]
+    batch.close()
+    for s, n in zip(solvers, steps):             # warm each context's own graph
+        s.reset_shot(0)
+        s.run(64)
+        s.reset_shot(0)
+
+    def singles():
+        for s, n in zip(solvers, steps):
+            s.run(n)
+    t_1 = timed(stream, singles)
+    same = all(np.array_equal(s.traces(0).view(np.uint32), t.view(np.uint32)) for s, t in zip(solvers, tr_b))
+    for s in solvers:
+        s.close()
+    sides = [sp["side"] for sp in specs]
+    return {"workload": "%d of the 256 uneven patchy models (seed %d): side U[256,1536] (here %d-%d), steps 4 x side, "
+                        "20-cell C-PML, 1 shot x 128 receivers x (vx,vz,p)" % (nmodels, seed, min(sides), max(sides)),
+            "cell_updates": work, "batched_gcells": work / t_b / 1e9, "back_to_back_gcells": work / t_1 / 1e9,
+            "speedup_vs_back_to_back": t_1 / t_b, "batched_s": t_b, "back_to_back_s": t_1,
+            "batched_launches": launches, "setup_s": setup, "first4_bitwise_equal_to_single_runs": same}
+
+
 def alg_bytes_per_step(g, s_ctx_strips, per_cell=96):
     """Algorithmic HBM bytes of one time step: per_cell bytes per cell plus
     8 B per C-PML memory variable on its strip (6 on x strips, 6 on z strips).
@@ -223,6 +341,9 @@ def main():
     ap.add_argument("--stencil", default="fast", choices=["fast", "exact"],
                     help="fast: plain FP32 stencils; exact: FP32 arithmetic rounded like the reference's FP64 lines")
     ap.add_argument("--no-parity", action="store_true", help="skip the fast-vs-exact drift check")
+    ap.add_argument("--batched", type=int, default=64, metavar="M",
+                    help="batched legs: 64 shots of one 1001x1001 model, and M of the 256 uneven models "
+                         "(0 skips both)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -344,6 +465,10 @@ def main():
     else:
         solver.close()
 
+    batched = None
+    if args.batched > 0:
+        batched = {"shots": leg_shots(P, stream, fast), "uneven": leg_uneven(P, stream, fast, args.batched)}
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_sample(g, coef, px, pz, src.ix, src.iz)
@@ -367,7 +492,7 @@ def main():
                          "palette_min_bytes_per_step": alg_pal,
                          "palette_frac": alg_pal / step_s / 1e9 / hbm},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity,
+            "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if pg:

@@ -204,6 +204,19 @@ int poe_get_derived_noalloc(poe_ctx *ctx, int32_t shot, int32_t field, float *ho
 /* Overwrite one full field of a shot (checkpoint restore; no reference counterpart). */
 int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in);
 
+/* Full-state checkpoint of one shot: no reference counterpart (the
+ * reference's vz/vx snapshots, cu:1653-1727, cannot restart a run).  The
+ * image holds a header (grid and C-PML layout, source, receiver count, step
+ * clock, checksum), every integrated field, the C-PML memory variables, the
+ * pressure-source accumulator and the traces recorded so far, in host byte
+ * order.  poe_checkpoint_load restores it into a shot of a context built
+ * with the same grid, profiles and shot definition (POE_EINVAL otherwise,
+ * POE_EIO on a checksum mismatch); running on from there gives the same
+ * fields and traces, bit for bit, as the uninterrupted run. */
+int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes);
+int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capacity);
+int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_t size);
+
 /* Steps completed by a shot. */
 int poe_steps_done(poe_ctx *ctx, int32_t shot, int64_t *steps);
 
@@ -221,6 +234,32 @@ int poe_kernel_launches(const poe_ctx *ctx, int64_t *count);
 const char *poe_last_error(const poe_ctx *ctx);
 const char *poe_status_string(int status);
 void poe_destroy(poe_ctx *ctx);
+
+/* ---------------------------------------------------------------- batches */
+
+/* A batch advances the shots of several contexts (models of any sizes) in one
+ * persistent launch per time step: no reference counterpart (the reference
+ * runs one shot of one model per process, cu:1596-1736).  Every context must
+ * be on the same device, use the material palette (few distinct materials, no
+ * POE_CTX_NO_PALETTE) and the same stencil mode.  The contexts stay owned by
+ * the caller and must outlive the batch; a context belongs to at most one
+ * batch at a time.  stream: a cudaStream_t or NULL for a private stream. */
+typedef struct poe_batch poe_batch;
+int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **out);
+
+/* Advance every shot of context i by nsteps[i] steps (nsteps[i] may differ and
+ * may be 0).  Results equal poe_run(ctxs[i], nsteps[i]) bit for bit.  Work
+ * after the batch on a context's own stream (poe_get_traces, poe_run) is
+ * ordered after it. */
+int poe_batch_run(poe_batch *b, const int64_t *nsteps);
+
+/* Wait for the batch; POE_ETIMEOUT if a kernel's bounded wait gave up. */
+int poe_batch_sync(poe_batch *b);
+
+/* Device kernels launched by this batch since creation. */
+int poe_batch_launches(const poe_batch *b, int64_t *count);
+const char *poe_batch_last_error(const poe_batch *b);
+void poe_batch_destroy(poe_batch *b);
 
 /* ---------------------------------------------------------------- reference geometry */
 

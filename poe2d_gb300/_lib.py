@@ -77,6 +77,9 @@ SYMBOLS = {
     "poe_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_get_derived_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
+    "poe_checkpoint_size": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
+    "poe_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "poe_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_reset_shot": (C.c_int, [C.c_void_p, C.c_int32]),
     "poe_check_finite": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, _fp]),
@@ -84,6 +87,12 @@ SYMBOLS = {
     "poe_last_error": (C.c_char_p, [C.c_void_p]),
     "poe_status_string": (C.c_char_p, [C.c_int]),
     "poe_destroy": (None, [C.c_void_p]),
+    "poe_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "poe_batch_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "poe_batch_sync": (C.c_int, [C.c_void_p]),
+    "poe_batch_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "poe_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "poe_batch_destroy": (None, [C.c_void_p]),
     "poe_ref_receivers": (C.c_int32, [C.POINTER(Grid), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.POINTER(Receiver), C.c_int32]),
 }

@@ -56,6 +56,10 @@ struct poe_ctx {
     StreamShot *shots_dev = nullptr;
     int64_t *steps_dev = nullptr;
     int shots_dev_cap = 0;
+    std::vector<StreamShot> shots_host;    // what shots_dev holds
+    std::vector<int4> items;               // palette mode: (0, shot, x0, z0) per tile and shot
+    int4 *items_dev = nullptr;
+    int items_dev_cap = 0;
     bool shots_dirty = true;
     int max_rec = 0;
     cudaGraphExec_t graph = nullptr;
@@ -189,11 +193,29 @@ int sync_shots(poe_ctx *ctx)
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
     }
+    // palette kernel work list: every tile of every shot, shot-major
+    ctx->items.clear();
+    if (ctx->ids)
+        for (int i = 0; i < ns; ++i)
+            for (int tz = 0; tz < ctx->ntz; ++tz)
+                for (int tx = 0; tx < ctx->ntx; ++tx) ctx->items.push_back(make_int4(0, i, tx * PAL_TX, tz * PAL_TZ));
+    const int ni = (int)ctx->items.size();
+    if (ni > ctx->items_dev_cap) {
+        cudaFree(ctx->items_dev);
+        ctx->items_dev = nullptr;
+        const int cap = std::max(ni, 2 * ctx->items_dev_cap);
+        CK(cudaMalloc(&ctx->items_dev, sizeof(int4) * cap));
+        ctx->items_dev_cap = cap;
+    }
     if (ns) {
         CK(cudaMemcpyAsync(ctx->shots_dev, sd.data(), sizeof(StreamShot) * ns, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaMemcpyAsync(ctx->steps_dev, st.data(), sizeof(int64_t) * ns, cudaMemcpyHostToDevice, ctx->stream));
+        if (ni)
+            CK(cudaMemcpyAsync(ctx->items_dev, ctx->items.data(), sizeof(int4) * ni, cudaMemcpyHostToDevice,
+                               ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));   // host vectors go out of scope
     }
+    ctx->shots_host = sd;
     drop_graph(ctx);
     ctx->shots_dirty = false;
     return POE_OK;
@@ -244,7 +266,8 @@ int kernels_per_step(const poe_ctx *) { return 1; }
 
 int step_launch(poe_ctx *ctx, int k)
 {
-    return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), k, ctx->exact, ctx->kone, ctx->stream);
+    return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), ctx->items_dev, (int)ctx->items.size(), k,
+                            ctx->exact, ctx->kone, ctx->stream);
 }
 
 int run_direct(poe_ctx *ctx, int64_t nsteps)
@@ -510,6 +533,7 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     ctx->tile_z = ctx->ids ? PAL_TZ : TILE_Z;
     ctx->ntx = (nx + ctx->tile_x - 1) / ctx->tile_x;
     ctx->ntz = (nz + ctx->tile_z - 1) / ctx->tile_z;
+    ctx->m.ntx = ctx->ntx;
     *out = ctx;
     return POE_OK;
 }
@@ -764,6 +788,172 @@ int poe_reset_shot(poe_ctx *ctx, int32_t shot)
     return sync_shots(ctx);
 }
 
+// ---- full-state checkpoints of one shot
+//
+// Layout: CkHeader, then (all float32, device layout incl. padding) the 9
+// integrated state planes of the current buffer, the x-strip and z-strip
+// C-PML memory of the stress update (current buffer) and of the velocity
+// update, the pressure-source accumulator (padded to 4 floats) and the
+// traces recorded so far (steps x nrec).  The other buffer of each pair is
+// not needed: step n reads buffer (n-1)&1 only.
+namespace {
+struct CkHeader {
+    char magic[8];          // "POE2DCK1"
+    uint32_t version, header_bytes;
+    int32_t NX, NZ, P, R, Wx, Hz;
+    int64_t plane, steps;
+    int32_t nrec, src_kind, src_ix, src_iz;
+    float f0, amplitude;
+    double t_cut;
+    int64_t payload_bytes;
+    uint64_t checksum;      // of the payload, 8-byte words
+    uint64_t reserved;
+};
+static_assert(sizeof(CkHeader) % 16 == 0, "header keeps the payload 16-byte aligned");
+
+uint64_t ck_sum(const unsigned char *p, size_t n)
+{
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t w;
+        std::memcpy(&w, p + i, 8);
+        h = (h ^ w) * 0x100000001b3ull;
+        h ^= h >> 29;
+    }
+    for (; i < n; ++i) h = (h ^ p[i]) * 0x100000001b3ull;
+    return h;
+}
+
+struct CkParts {
+    size_t f, x, z, acc, tr;
+};
+
+CkParts ck_parts(const poe_ctx *ctx, const ShotHost &s)
+{
+    const ModelDev &m = ctx->m;
+    CkParts c;
+    c.f = sizeof(float) * m.plane * NSF;
+    c.x = s.mxv ? sizeof(float) * 3 * (size_t)(m.NZ + 1) * m.Wx : 0;
+    c.z = s.mzv ? sizeof(float) * 3 * (size_t)m.Hz * m.P : 0;
+    c.acc = 4 * sizeof(float);
+    c.tr = sizeof(float) * (size_t)s.steps * s.nrec;
+    return c;
+}
+
+size_t ck_payload(const CkParts &c) { return c.f + 2 * c.x + 2 * c.z + c.acc + c.tr; }
+
+void ck_fill_header(const poe_ctx *ctx, const ShotHost &s, CkHeader &h)
+{
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, "POE2DCK1", 8);
+    h.version = 1;
+    h.header_bytes = sizeof(CkHeader);
+    const ModelDev &m = ctx->m;
+    h.NX = m.NX;
+    h.NZ = m.NZ;
+    h.P = m.P;
+    h.R = m.R;
+    h.Wx = m.Wx;
+    h.Hz = m.Hz;
+    h.plane = m.plane;
+    h.steps = s.steps;
+    h.nrec = s.nrec;
+    h.src_kind = s.src_where == SRC_NONE ? -1 : s.src.kind;
+    h.src_ix = s.src_where == SRC_NONE ? 0 : s.src.ix;
+    h.src_iz = s.src_where == SRC_NONE ? 0 : s.src.iz;
+    h.f0 = s.src_where == SRC_NONE ? 0.0f : s.src.f0;
+    h.amplitude = s.src_where == SRC_NONE ? 0.0f : s.src.amplitude;
+    h.t_cut = s.src_where == SRC_NONE ? 0.0 : s.src.t_cut;
+}
+}  // namespace
+
+int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s || !bytes) return fail(ctx, POE_EINVAL, "shot id");
+    *bytes = (int64_t)(sizeof(CkHeader) + ck_payload(ck_parts(ctx, *s)));
+    return POE_OK;
+}
+
+int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capacity)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    const CkParts c = ck_parts(ctx, *s);
+    const size_t need = sizeof(CkHeader) + ck_payload(c);
+    if (!host_buf || capacity < (int64_t)need) return fail(ctx, POE_EINVAL, "checkpoint buffer too small");
+    CK(cudaSetDevice(ctx->device));
+    const int b = (int)(s->steps & 1);
+    unsigned char *p = static_cast<unsigned char *>(host_buf) + sizeof(CkHeader);
+    auto get = [&](const void *src, size_t n) -> int {
+        if (n) CK(cudaMemcpyAsync(p, src, n, cudaMemcpyDeviceToHost, ctx->stream));
+        p += n;
+        return POE_OK;
+    };
+    int rc;
+    if ((rc = get(s->f[b], c.f)) || (rc = get(s->mx[b], c.x)) || (rc = get(s->mxv, c.x)) ||
+        (rc = get(s->mz[b], c.z)) || (rc = get(s->mzv, c.z)))
+        return rc;
+    std::memset(p, 0, c.acc);
+    if ((rc = get(s->acc + b, sizeof(float)))) return rc;
+    p += c.acc - sizeof(float);
+    if ((rc = get(s->trace, c.tr))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if ((rc = device_status(ctx)) != POE_OK) return rc;
+    CkHeader h;
+    ck_fill_header(ctx, *s, h);
+    h.payload_bytes = (int64_t)ck_payload(c);
+    h.checksum = ck_sum(static_cast<unsigned char *>(host_buf) + sizeof(CkHeader), ck_payload(c));
+    std::memcpy(host_buf, &h, sizeof h);
+    return POE_OK;
+}
+
+int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_t size)
+{
+    ShotHost *s = get_shot(ctx, shot);
+    if (!s) return fail(ctx, POE_EINVAL, "shot id");
+    if (!host_buf || size < (int64_t)sizeof(CkHeader)) return fail(ctx, POE_EINVAL, "checkpoint too short");
+    CkHeader h, want;
+    std::memcpy(&h, host_buf, sizeof h);
+    if (std::memcmp(h.magic, "POE2DCK1", 8) || h.version != 1 || h.header_bytes != sizeof(CkHeader))
+        return fail(ctx, POE_EINVAL, "not a poe2d checkpoint (version 1)");
+    ck_fill_header(ctx, *s, want);
+    if (h.NX != want.NX || h.NZ != want.NZ || h.P != want.P || h.R != want.R || h.Wx != want.Wx ||
+        h.Hz != want.Hz || h.plane != want.plane)
+        return fail(ctx, POE_EINVAL, "checkpoint of another grid or C-PML layout");
+    if (h.nrec != want.nrec || h.src_kind != want.src_kind || h.src_ix != want.src_ix || h.src_iz != want.src_iz ||
+        h.f0 != want.f0 || h.amplitude != want.amplitude || h.t_cut != want.t_cut)
+        return fail(ctx, POE_EINVAL, "checkpoint of another shot (source or receiver count differ)");
+    if (h.steps < 0) return fail(ctx, POE_EINVAL, "checkpoint step count");
+    const int64_t keep = s->steps;
+    s->steps = h.steps;
+    const CkParts c = ck_parts(ctx, *s);
+    s->steps = keep;
+    if (h.payload_bytes != (int64_t)ck_payload(c) || size < (int64_t)(sizeof(CkHeader) + ck_payload(c)))
+        return fail(ctx, POE_EINVAL, "checkpoint size");
+    const unsigned char *p = static_cast<const unsigned char *>(host_buf) + sizeof(CkHeader);
+    if (ck_sum(p, ck_payload(c)) != h.checksum) return fail(ctx, POE_EIO, "checkpoint checksum mismatch");
+    int rc;
+    if ((rc = poe_reset_shot(ctx, shot)) != POE_OK) return rc;   // both buffers and traces zero, clock 0
+    if ((rc = ensure_trace(ctx, *s, h.steps)) != POE_OK) return rc;
+    const int b = (int)(h.steps & 1);
+    auto put = [&](void *dst, size_t n) -> int {
+        if (n) CK(cudaMemcpyAsync(dst, p, n, cudaMemcpyHostToDevice, ctx->stream));
+        p += n;
+        return POE_OK;
+    };
+    if ((rc = put(s->f[b], c.f)) || (rc = put(s->mx[b], c.x)) || (rc = put(s->mxv, c.x)) ||
+        (rc = put(s->mz[b], c.z)) || (rc = put(s->mzv, c.z)) || (rc = put(s->acc + b, sizeof(float))))
+        return rc;
+    p += c.acc - sizeof(float);
+    if ((rc = put(s->trace, c.tr))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    s->steps = h.steps;
+    ctx->shots_dirty = true;
+    return sync_shots(ctx);
+}
+
 int poe_check_finite(poe_ctx *ctx, int32_t shot, float threshold, float *max_abs_out)
 {
     ShotHost *s = get_shot(ctx, shot);
@@ -802,6 +992,7 @@ void poe_destroy(poe_ctx *ctx)
     for (ShotHost &s : ctx->shots) free_shot(s);
     cudaFree(ctx->shots_dev);
     cudaFree(ctx->steps_dev);
+    cudaFree(ctx->items_dev);
     cudaFree(ctx->coef);
     cudaFree(ctx->px);
     cudaFree(ctx->pz);
@@ -811,6 +1002,264 @@ void poe_destroy(poe_ctx *ctx)
     cudaFree(ctx->mtab);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- batches
+//
+// A batch concatenates the work lists of its contexts: item (model, shot, x0,
+// z0) with model indexing the batch's ModelDev array and shot its StreamShot
+// array.  Contexts are ordered by steps requested (most first), so the items of
+// the contexts still running are always a prefix of the list: a run is a few
+// segments, each launching over a shorter prefix, and no kernel tests whether
+// its model is finished.
+
+struct poe_batch {
+    std::vector<poe_ctx *> ctxs;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    bool exact = true, kone = true;
+    ModelDev *models_dev = nullptr;
+    StreamShot *shots_dev = nullptr;
+    int4 *items_dev = nullptr;
+    int models_cap = 0, shots_cap = 0, items_cap = 0;
+    std::vector<std::array<int, 2>> graph_keys;   // (items, shots) prefix of each graph
+    std::vector<cudaGraphExec_t> graphs;
+    cudaEvent_t done = nullptr;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int bfail(poe_batch *b, int code, const std::string &msg)
+{
+    if (b) b->err = msg;
+    return code;
+}
+
+#define BK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return bfail(b, e_ == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,    \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));            \
+    } while (0)
+
+void drop_batch_graphs(poe_batch *b)
+{
+    for (cudaGraphExec_t g : b->graphs) cudaGraphExecDestroy(g);
+    b->graphs.clear();
+    b->graph_keys.clear();
+}
+
+template <class T>
+int grow(poe_batch *b, T **p, int &cap, int need)
+{
+    if (need <= cap) return POE_OK;
+    drop_batch_graphs(b);   // graphs hold the old pointers
+    const int c = std::max(need, 2 * cap);
+    cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    BK(cudaMalloc(p, sizeof(T) * c));
+    cap = c;
+    return POE_OK;
+}
+
+int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
+{
+    for (int64_t k = 0; k < nsteps; ++k) {
+        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->kone,
+                                        b->stream);
+        if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
+    }
+    const int r = launch_advance_shots(b->shots_dev, nshots, nsteps, b->stream);
+    if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
+    b->launches += nsteps + 1;
+    return POE_OK;
+}
+
+cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
+{
+    for (size_t i = 0; i < b->graph_keys.size(); ++i)
+        if (b->graph_keys[i][0] == nitems && b->graph_keys[i][1] == nshots) return b->graphs[i];
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+    int rc = 0;
+    for (int k = 0; k < kGraphSteps && rc == 0; ++k)
+        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->kone, b->stream);
+    if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc != 0 || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return nullptr;
+    }
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return nullptr;
+    b->graph_keys.push_back({nitems, nshots});
+    b->graphs.push_back(x);
+    return x;
+}
+
+int batch_segment(poe_batch *b, int nitems, int nshots, int64_t nsteps)
+{
+    int64_t left = nsteps;
+    if (left >= kGraphSteps) {
+        cudaGraphExec_t g = batch_graph(b, nitems, nshots);
+        if (!g) return bfail(b, POE_ECUDA, "batch graph capture failed");
+        for (; left >= kGraphSteps; left -= kGraphSteps) {
+            BK(cudaGraphLaunch(g, b->stream));
+            b->launches += kGraphSteps + 1;
+        }
+    }
+    return left > 0 ? batch_steps(b, nitems, nshots, left) : POE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **out)
+{
+    if (!out) return POE_EINVAL;
+    *out = nullptr;
+    if (!ctxs || n <= 0) return POE_EINVAL;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i]) return POE_EINVAL;
+        if (!ctxs[i]->ids) return fail(ctxs[i], POE_EINVAL, "batch: context without a material palette");
+        if (ctxs[i]->device != ctxs[0]->device) return fail(ctxs[i], POE_EINVAL, "batch: contexts on other devices");
+        if (ctxs[i]->exact != ctxs[0]->exact) return fail(ctxs[i], POE_EINVAL, "batch: mixed stencil modes");
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(ctxs[i], POE_EINVAL, "batch: context listed twice");
+    }
+    poe_batch *b = new poe_batch;
+    b->ctxs.assign(ctxs, ctxs + n);
+    b->device = ctxs[0]->device;
+    b->exact = ctxs[0]->exact;
+    for (poe_ctx *c : b->ctxs) b->kone = b->kone && c->kone;   // K = 1 divides are exact: KONE=false is safe
+    if (cudaSetDevice(b->device) != cudaSuccess) {
+        delete b;
+        return POE_ECUDA;
+    }
+    if (stream) {
+        b->stream = (cudaStream_t)stream;
+    } else if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess) {
+        b->own_stream = true;
+    } else {
+        delete b;
+        return POE_ECUDA;
+    }
+    if (cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
+        poe_batch_destroy(b);
+        return POE_ECUDA;
+    }
+    *out = b;
+    return POE_OK;
+}
+
+int poe_batch_run(poe_batch *b, const int64_t *nsteps)
+{
+    if (!b) return POE_EINVAL;
+    if (!nsteps) return bfail(b, POE_EINVAL, "nsteps");
+    const int n = (int)b->ctxs.size();
+    for (int i = 0; i < n; ++i) {
+        if (nsteps[i] < 0) return bfail(b, POE_EINVAL, "nsteps < 0");
+        if (nsteps[i] > 0 && b->ctxs[i]->shots.empty()) return bfail(b, POE_ESTATE, "a context has no shots");
+    }
+    BK(cudaSetDevice(b->device));
+    BK(cudaStreamSynchronize(b->stream));   // the previous run still reads the work list
+    std::vector<int> order;
+    for (int i = 0; i < n; ++i) {
+        if (nsteps[i] == 0) continue;
+        poe_ctx *ctx = b->ctxs[i];
+        int rc;
+        for (ShotHost &s : ctx->shots) {
+            if ((rc = ensure_trace(ctx, s, s.steps + nsteps[i])) != POE_OK) return bfail(b, rc, ctx->err);
+            if ((rc = ensure_source(ctx, s, s.steps + nsteps[i])) != POE_OK) return bfail(b, rc, ctx->err);
+        }
+        if ((rc = sync_shots(ctx)) != POE_OK) return bfail(b, rc, ctx->err);
+        BK(cudaStreamSynchronize(ctx->stream));   // earlier work on the context's own stream
+        order.push_back(i);
+    }
+    if (order.empty()) return POE_OK;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return nsteps[a] > nsteps[c]; });
+
+    // concatenated work list; item_end[p] / shot_end[p]: prefix sizes through context order[p]
+    std::vector<ModelDev> hm;
+    std::vector<StreamShot> hs;
+    std::vector<int4> hi;
+    std::vector<int> item_end, shot_end;
+    for (int p = 0; p < (int)order.size(); ++p) {
+        const poe_ctx *ctx = b->ctxs[order[p]];
+        const int shot0 = (int)hs.size();
+        hm.push_back(ctx->m);
+        hs.insert(hs.end(), ctx->shots_host.begin(), ctx->shots_host.end());
+        for (int4 it : ctx->items) hi.push_back(make_int4(p, shot0 + it.y, it.z, it.w));
+        item_end.push_back((int)hi.size());
+        shot_end.push_back((int)hs.size());
+    }
+    int rc;
+    if ((rc = grow(b, &b->models_dev, b->models_cap, (int)hm.size())) != POE_OK) return rc;
+    if ((rc = grow(b, &b->shots_dev, b->shots_cap, (int)hs.size())) != POE_OK) return rc;
+    if ((rc = grow(b, &b->items_dev, b->items_cap, (int)hi.size())) != POE_OK) return rc;
+    BK(cudaMemcpyAsync(b->models_dev, hm.data(), sizeof(ModelDev) * hm.size(), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->shots_dev, hs.data(), sizeof(StreamShot) * hs.size(), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->items_dev, hi.data(), sizeof(int4) * hi.size(), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaStreamSynchronize(b->stream));   // host vectors go out of scope
+
+    int64_t done = 0;
+    for (int p = (int)order.size() - 1; p >= 0; --p) {   // segment: contexts order[0..p] still running
+        const int64_t until = nsteps[order[p]];
+        if (until > done) {
+            if ((rc = batch_segment(b, item_end[p], shot_end[p], until - done)) != POE_OK) return rc;
+            done = until;
+        }
+    }
+    BK(cudaEventRecord(b->done, b->stream));
+    for (int i : order) {
+        poe_ctx *ctx = b->ctxs[i];
+        BK(cudaStreamWaitEvent(ctx->stream, b->done, 0));
+        for (ShotHost &s : ctx->shots) s.steps += nsteps[i];
+    }
+    return POE_OK;
+}
+
+int poe_batch_sync(poe_batch *b)
+{
+    if (!b) return POE_EINVAL;
+    BK(cudaStreamSynchronize(b->stream));
+    for (poe_ctx *ctx : b->ctxs) {
+        const int rc = device_status(ctx);
+        if (rc != POE_OK) return bfail(b, rc, ctx->err);
+    }
+    return POE_OK;
+}
+
+int poe_batch_launches(const poe_batch *b, int64_t *count)
+{
+    if (!b || !count) return POE_EINVAL;
+    *count = b->launches;
+    return POE_OK;
+}
+
+const char *poe_batch_last_error(const poe_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+void poe_batch_destroy(poe_batch *b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_batch_graphs(b);
+    cudaFree(b->models_dev);
+    cudaFree(b->shots_dev);
+    cudaFree(b->items_dev);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    delete b;
 }
 
 }  // extern "C"

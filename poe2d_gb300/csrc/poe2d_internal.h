@@ -52,6 +52,7 @@ struct ModelDev {
     const uint8_t *ids;      // padded plane of material ids (pitch P bytes, R rows), or null
     const float *mtab;       // nmat rows of MT_W floats
     int nmat;
+    int ntx;                 // tiles across x of the kernel this model runs on (receiver lists)
 };
 
 // material-table row: coefficients and the quantities the reference derives
@@ -107,8 +108,15 @@ struct StreamShot {
     const void *tm_s;
 };
 
-int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, int k, bool exact, bool kone,
-                     void *stream);
+// one step of a model's shots; palette models take the work list items[0..nitems)
+// of (0, shot, x0, z0)
+int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
+                     bool exact, bool kone, void *stream);
+// one step over several palette models: items (model, shot, x0, z0) index models_dev and shots_dev
+int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
+                      bool exact, bool kone, void *stream);
+// *shots[i].step += by for i < nshots
+int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
 // palette kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
 // columns = tile + 2-cell halo each side); TMA boxes of 68 x 40 (velocity) and
 // 68 x 36 (stress state) floats

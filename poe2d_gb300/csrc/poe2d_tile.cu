@@ -417,31 +417,25 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 }  // namespace
 
-template <bool EXACT, bool KONE>
+template <bool EXACT, bool KONE, bool MULTI>
 __global__ void __launch_bounds__(PNT, 1)
-k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx, int ntiles, int nitems)
+k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
+           const int4 *__restrict__ items, int nitems, int k)
 {
     extern __shared__ __align__(128) unsigned char smp[];
     float *st = reinterpret_cast<float *>(smp + PAL_OFF_T);     // nmat x MT_W
     uint64_t *bar = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     const int tid = threadIdx.x;
     const int lx = tid & 63, ly = tid >> 6;                      // 64 x 8 thread grid
-    const int NX = m.NX, NZ = m.NZ;
-    const int P = m.P;
-    const int64_t PL = m.plane;
-    const float dt = m.dt;
-    const float *__restrict__ PX = m.px;
-    const float *__restrict__ PZ = m.pz;
-    const int R = m.R;
-    const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
 
-    // fill buffer b with work item w (thread 0 issues the TMA batch; everyone
-    // issues cp.async for the ids)
+    // fill buffer b with work item w = (model, shot, x0, z0): thread 0 issues
+    // the TMA batch, everyone issues cp.async for the ids
     auto issue = [&](int w, int b) {
-        const int shot = w / ntiles, tile = w - shot * ntiles;
-        const StreamShot &S = shots[shot];
-        const int tx = tile % ntx, tz = tile / ntx;
-        const int x0 = tx * QX, z0 = tz * QZ;
+        const int4 it = items[w];
+        const ModelDev &m = MULTI ? models[it.x] : mp;
+        const StreamShot &S = shots[it.y];
+        const int x0 = it.z, z0 = it.w;
+        const int P = m.P;
         unsigned char *buf = smp + b * BUF_BYTES;
         if (tid == 0) {
             const int64_t n = *S.step + k + 1;
@@ -471,13 +465,23 @@ k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int nt
         mbar_init(&bar[1], 1);
         mbar_fence_init();
     }
-    for (int i = tid; i < m.nmat * MT_W; i += PNT) st[i] = m.mtab[i];
+    int table_of = -1;                     // model whose material table is in shared memory
+    if (!MULTI) {
+        for (int i = tid; i < mp.nmat * MT_W; i += PNT) st[i] = mp.mtab[i];
+        table_of = 0;
+    }
     __syncthreads();
     int w = blockIdx.x;
     if (w < nitems) issue(w, 0);
 
     for (int j = 0; w < nitems; ++j, w += gridDim.x) {
         const int b = j & 1;
+        const int4 it = items[w];
+        const ModelDev &m = MULTI ? models[it.x] : mp;
+        if (MULTI && it.x != table_of) {   // the previous item's compute is over (trailing barrier)
+            for (int i = tid; i < m.nmat * MT_W; i += PNT) st[i] = m.mtab[i];
+            table_of = it.x;
+        }
         const bool ok = mbar_wait(&bar[b], (uint32_t)((j >> 1) & 1));
         cp_async_wait_all();
         if (!__syncthreads_and(ok)) {     // a bounded wait gave up: report, drain, leave
@@ -485,14 +489,21 @@ k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int nt
             if (w + (int)gridDim.x < nitems) mbar_wait(&bar[b ^ 1], (uint32_t)(((j + 1) >> 1) & 1));
             return;
         }
-        if (w + (int)gridDim.x < nitems) issue(w + gridDim.x, b ^ 1);   // buffer b^1 is free: tile j-1 done
+        if (w + (int)gridDim.x < nitems) issue(w + gridDim.x, b ^ 1);   // buffer b^1 is free: item j-1 done
 
-        const int shot = w / ntiles, tile = w - shot * ntiles;
-        const StreamShot &S = shots[shot];
+        const int NX = m.NX, NZ = m.NZ;
+        const int P = m.P;
+        const int64_t PL = m.plane;
+        const float dt = m.dt;
+        const float *__restrict__ PX = m.px;
+        const float *__restrict__ PZ = m.pz;
+        const int R = m.R;
+        const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
+        const StreamShot &S = shots[it.y];
         const int64_t n = *S.step + k + 1;
         const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
-        const int tx = tile % ntx, tz = tile / ntx;
-        const int x0 = tx * QX, z0 = tz * QZ;
+        const int x0 = it.z, z0 = it.w;
+        const int tile = (z0 / QZ) * m.ntx + x0 / QX;
         float *__restrict__ FB = S.f[wr];
         const int src_off = (int)S.src_off;
         const int src_where = S.src_where;
@@ -728,44 +739,90 @@ k_tile_pal(const ModelDev m, const StreamShot *__restrict__ shots, int k, int nt
 }
 
 namespace {
+int sm_count()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
 constexpr size_t TILE_SMEM = sizeof(float) * (4 * V_FLOATS + 4 * S_FLOATS);
 
 template <bool EXACT, bool KONE>
-int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, int k, cudaStream_t st)
+int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4 *items, int nitems, int k,
+              cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_tile<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TILE_SMEM);
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAL_SMEM);
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PAL_SMEM);
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PAL_SMEM);
         attr = true;
     }
     if (m.ids) {
-        const int ntx = (m.NX + 1 + PAL_TX - 1) / PAL_TX, ntz = (m.NZ + 1 + PAL_TZ - 1) / PAL_TZ;
-        const int nitems = ntx * ntz * nshots;
-        static int sms = 0;
-        if (!sms) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        }
-        const int grid = nitems < sms ? nitems : sms;   // persistent: one CTA per SM
-        k_tile_pal<EXACT, KONE><<<grid, PNT, PAL_SMEM, st>>>(m, shots, k, ntx, ntx * ntz, nitems);
+        const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
+        if (grid > 0) k_tile_pal<EXACT, KONE, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
     } else {
         const int ntx = (m.NX + 1 + TX - 1) / TX, ntz = (m.NZ + 1 + TZ - 1) / TZ;
         k_tile<EXACT, KONE><<<dim3(ntx * ntz, nshots), NT, TILE_SMEM, st>>>(m, shots, k, ntx);
     }
     return (int)cudaGetLastError();
 }
+
+template <bool EXACT, bool KONE>
+int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems, int k, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)PAL_SMEM);
+        attr = true;
+    }
+    const int grid = nitems < sm_count() ? nitems : sm_count();
+    ModelDev dummy{};
+    if (grid > 0) k_tile_pal<EXACT, KONE, true><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    return (int)cudaGetLastError();
+}
 }  // namespace
 
-int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, int k, bool exact, bool kone,
-                     void *stream)
+int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
+                     bool exact, bool kone, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (exact) return kone ? tile_impl<true, true>(m, shots_dev, nshots, k, st)
-                           : tile_impl<true, false>(m, shots_dev, nshots, k, st);
-    return kone ? tile_impl<false, true>(m, shots_dev, nshots, k, st)
-                : tile_impl<false, false>(m, shots_dev, nshots, k, st);
+    if (exact) return kone ? tile_impl<true, true>(m, shots_dev, nshots, items, nitems, k, st)
+                           : tile_impl<true, false>(m, shots_dev, nshots, items, nitems, k, st);
+    return kone ? tile_impl<false, true>(m, shots_dev, nshots, items, nitems, k, st)
+                : tile_impl<false, false>(m, shots_dev, nshots, items, nitems, k, st);
+}
+
+int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
+                      bool exact, bool kone, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (exact) return kone ? batch_impl<true, true>(models_dev, shots_dev, items, nitems, k, st)
+                           : batch_impl<true, false>(models_dev, shots_dev, items, nitems, k, st);
+    return kone ? batch_impl<false, true>(models_dev, shots_dev, items, nitems, k, st)
+                : batch_impl<false, false>(models_dev, shots_dev, items, nitems, k, st);
+}
+
+__global__ void k_advance_shots(const StreamShot *shots, int nshots, int64_t by)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nshots) *const_cast<int64_t *>(shots[i].step) += by;
+}
+
+int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream)
+{
+    if (nshots <= 0) return 0;
+    k_advance_shots<<<(nshots + 127) / 128, 128, 0, (cudaStream_t)stream>>>(shots_dev, nshots, by);
+    return (int)cudaGetLastError();
 }
 
 // ---- small helpers: step counters and derived fields ----

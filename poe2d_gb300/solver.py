@@ -197,6 +197,19 @@ class Solver:
         a = np.ascontiguousarray(np.asarray(values, np.float32).reshape(self.shape))
         self._check(L.lib().poe_set_field(self.h, shot, fid, _f(a)))
 
+    def checkpoint(self, shot=0):
+        """Full state of a shot as bytes (fields, C-PML memory, traces, clock)."""
+        n = C.c_int64(0)
+        self._check(L.lib().poe_checkpoint_size(self.h, shot, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        self._check(L.lib().poe_checkpoint_save(self.h, shot, buf.ctypes.data_as(C.c_void_p), n.value))
+        return buf.tobytes()
+
+    def restore(self, image, shot=0):
+        """Load a checkpoint() image into a shot with the same definition."""
+        buf = np.frombuffer(image, np.uint8)
+        self._check(L.lib().poe_checkpoint_load(self.h, shot, buf.ctypes.data_as(C.c_void_p), buf.size))
+
     def reset_shot(self, shot=0):
         self._check(L.lib().poe_reset_shot(self.h, shot))
 
@@ -210,3 +223,63 @@ class Solver:
         n = C.c_int64(0)
         self._check(L.lib().poe_kernel_launches(self.h, C.byref(n)))
         return n.value
+
+
+class Batch:
+    """Several Solvers advanced together, one persistent launch per time step.
+
+    Every solver must use the material palette (the default for patchy
+    models) and the same stencil mode.  run(steps) takes one step count per
+    solver (or one for all); each solver's shots end exactly as after
+    solver.run(steps[i]).  The solvers must outlive the batch.
+    """
+
+    def __init__(self, solvers, stream=None):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = C.c_void_p()
+        st = L.lib().poe_batch_create(arr, len(self.solvers), C.c_void_p(stream or 0), C.byref(h))
+        if st != L.POE_OK:
+            msg = ""
+            for s in self.solvers:
+                m = L.lib().poe_last_error(s.h)
+                if m:
+                    msg = m.decode()
+            raise PoeError(st, msg)
+        self.h = h
+
+    def _check(self, st):
+        if st != L.POE_OK:
+            m = L.lib().poe_batch_last_error(self.h)
+            raise PoeError(st, m.decode() if m else "")
+
+    def run(self, steps):
+        if np.isscalar(steps):
+            steps = [int(steps)] * len(self.solvers)
+        if len(steps) != len(self.solvers):
+            raise PoeError(L.POE_EINVAL, "one step count per solver")
+        arr = (C.c_int64 * len(steps))(*[int(v) for v in steps])
+        self._check(L.lib().poe_batch_run(self.h, arr))
+
+    def sync(self):
+        self._check(L.lib().poe_batch_sync(self.h))
+
+    @property
+    def launches(self):
+        n = C.c_int64(0)
+        self._check(L.lib().poe_batch_launches(self.h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().poe_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

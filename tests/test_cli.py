@@ -1,0 +1,127 @@
+"""The drop-in driver poe2d_run: the reference program's inputs and outputs.
+
+CPU tests use --dry-run (inputs read and checked, coefficients and C-PML
+profiles built, mediumrho.ctxt written, no GPU).  The GPU test runs a small
+model end to end and checks every output file, byte for byte, against the
+same run through the library (traces, snapshots) formatted the way the
+reference's std::ofstream prints floats (cu:1772-1905).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from poe2d_gb300 import build as B
+
+NX, NZ = 119, 99
+
+
+def _cli():
+    B.build()
+    assert os.path.exists(B.CLI)
+    return B.CLI
+
+
+def _write_case(d, order="x", nstep=130, isrc=60, jsrc=50, f0=200.0, ids=None):
+    from poe2d_gb300.patchy import write_bin
+    rng = np.random.default_rng(5)
+    sh = (NZ + 1, NX + 1)
+    medium = (ids if ids is not None else rng.integers(0, 4, size=sh)).astype(np.float32)
+    cp = rng.uniform(2600, 3300, size=sh).astype(np.float32)
+    cs = rng.uniform(1300, 1700, size=sh).astype(np.float32)
+    rho = rng.uniform(2100, 2500, size=sh).astype(np.float32)
+    for name, a in (("m.bin", medium), ("cp.bin", cp), ("cs.bin", cs), ("rho.bin", rho)):
+        write_bin(os.path.join(d, name), a, order=order)
+    with open(os.path.join(d, "input1.txt"), "w") as f:
+        f.write("%d\n%d %d\n%d\n%d\n" % (nstep, isrc, jsrc, 30, 70))
+    with open(os.path.join(d, "input2.txt"), "w") as f:
+        f.write("%g\n" % f0)
+    # stable poroelastic fluids (the reference's own table is its elastic limit, phi = 1e-6)
+    from tests.golden.make_golden import LOOP_TABLE
+    np.savetxt(os.path.join(d, "fluid.txt"), np.asarray(LOOP_TABLE, np.float64), fmt="%.9g")
+    return medium, cp, cs, rho
+
+
+def _args(d, order="x", extra=()):
+    return [_cli(), "--nx", str(NX), "--nz", str(NZ), "--dx", "0.5", "--dt", "5e-5", "--panj", "10", "--panj2",
+            "12", "--samp", "64", "--npml", "10", "--medium", "m.bin", "--cp", "cp.bin", "--cs", "cs.bin", "--rho",
+            "rho.bin", "--order", order, "--fluid", os.path.join(d, "fluid.txt"), "--in", d, "--out", d] + list(extra)
+
+
+def test_missing_inputs_message(tmp_path):
+    r = subprocess.run([_cli(), "--in", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 1 and "File not opened..." in r.stdout
+
+
+@pytest.mark.parametrize("order", ["x", "z"])
+def test_dry_run_reads_both_orders(tmp_path, order):
+    d = str(tmp_path)
+    medium, cp, cs, rho = _write_case(d, order)
+    r = subprocess.run(_args(d, order, ["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "grid 120 x 100" in r.stdout
+    dump = np.fromfile(os.path.join(d, "mediumrho.ctxt"), "<f4").reshape(NZ + 1, NX + 1)
+    assert np.array_equal(dump, cp)          # cu:1476-1487 writes cp, x fastest
+
+
+def test_bad_medium_id_and_short_file(tmp_path):
+    d = str(tmp_path)
+    ids = np.zeros((NZ + 1, NX + 1))
+    ids[3, 4] = 7                             # no fluid row 7
+    _write_case(d, ids=ids)
+    r = subprocess.run(_args(d, extra=["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 1 and "medium" in r.stderr
+    _write_case(d)
+    with open(os.path.join(d, "cs.bin"), "r+b") as f:
+        f.truncate(100)
+    r = subprocess.run(_args(d, extra=["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 1 and "expected" in r.stderr
+
+
+def test_courant_failure_returns_like_the_reference(tmp_path):
+    d = str(tmp_path)
+    _write_case(d)
+    args = _args(d, extra=["--dry-run"])
+    args[args.index("--dt") + 1] = "5e-4"
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0 and "time step is too large" in r.stdout
+
+
+def _fmt_rows(a):
+    return "".join("".join("%g " % float(v) for v in row) + "\n" for row in a)
+
+
+@pytest.mark.gpu
+def test_cli_outputs_match_library_run(tmp_path, poe):
+    d = str(tmp_path)
+    nstep, isrc, jsrc, f0 = 130, 60, 50, 200.0
+    medium, cp, cs, rho = _write_case(d, "z", nstep, isrc, jsrc, f0)
+    r = subprocess.run(_args(d, "z"), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+    from tests.golden.make_golden import LOOP_TABLE
+    g = poe.grid(NX, NZ, 0.5, 5e-5)
+    coef = poe.coeffs_from_medium(g, medium, cp, cs, rho, LOOP_TABLE)
+    px, pz = poe.pml_profiles(g, 10, f0, float(cp.max()))
+    rec = poe.ref_receivers(g, isrc, jsrc, 10, 12, 30, 70)
+    with poe.Solver(g, coef, px, pz) as s:
+        s.add_shot(poe.source(isrc, jsrc, poe.SRC_REF_DGAUSS_P, f0, 1.0, 0.4), rec)
+        snaps = {}
+        for k in (64, 128):
+            s.run(k - s.steps())
+            snaps[k] = (s.field("vz"), s.field("vx"))
+        s.run(nstep - s.steps())
+        tr = s.traces()
+    for k, (vz, vx) in snaps.items():
+        assert np.array_equal(np.fromfile(os.path.join(d, "vz%05d.vzo" % k), "<f4").reshape(vz.shape), vz)
+        assert np.array_equal(np.fromfile(os.path.join(d, "vx%05d.vxo" % k), "<f4").reshape(vx.shape), vx)
+    assert not os.path.exists(os.path.join(d, "vz%05d.vzo" % 130))
+    cols = {"recvspvz%08d.vsp": tr[:, 0:10], "recvspvx%08d.vsp": tr[:, 10:20], "rechorvz%08d.hor": tr[:, 20:32],
+            "rechorvx%08d.hor": tr[:, 32:44]}
+    for pat, a in cols.items():
+        with open(os.path.join(d, pat % int(f0))) as f:
+            assert f.read() == _fmt_rows(a), pat
+    for i, pat in enumerate(("recats%08d.ats", "recbwh%08d.bwh", "recsrc%08d.src")):
+        with open(os.path.join(d, pat % int(f0))) as f:
+            assert f.read() == "".join("%g " % float(v) for v in tr[:, 45 + i]), pat

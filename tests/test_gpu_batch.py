@@ -1,0 +1,108 @@
+"""Batched solver: several models of uneven sizes and step counts in one
+persistent launch per step must end exactly where separate runs end.
+
+The batch kernel is the palette kernel over a concatenated work list
+(model, shot, tile); each model reads its own grid, profiles and material
+table, so the comparison with single-context runs is bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _patchy(poe, NX, NZ, seed, phi=0.2):
+    from poe2d_gb300.patchy import random_patches
+    frame = dict(rho_s=2650.0, phi=phi, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = poe.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    gas = poe.biot_material(rho_f=100.0, k_f=0.02e9, eta=1e-5, **frame)
+    ids = random_patches((NZ + 1, NX + 1), 0.5, fraction=0.2, r_min=1.0, r_max=4.0, seed=seed)
+    return poe.coeffs_biot([water, gas], ids)
+
+
+# (NX, NZ, npml, k_max, shots, f0): uneven sizes, one model with K != 1 in its C-PML
+MODELS = [(130, 97, 10, 1.0, 2, 200.0), (251, 201, 12, 1.0, 1, 250.0), (77, 181, 8, 1.5, 1, 180.0),
+          (190, 60, 6, 1.0, 2, 300.0), (300, 33, 5, 1.0, 1, 220.0)]
+
+
+def _build(poe, fast):
+    out = []
+    for i, (NX, NZ, npml, kmax, nshots, f0) in enumerate(MODELS):
+        coef, vp = _patchy(poe, NX, NZ, 40 + i, phi=0.15 + 0.03 * i)
+        g = poe.grid(NX, NZ, 0.5, 5e-5)
+        par = poe.pml_defaults(npml, f0, vp)
+        par.k_max = kmax
+        px, pz = poe.pml_profiles(g, params=par)
+        rec = [(x, 3 + npml, c) for c in (0, 1, 2) for x in range(2, NX - 1, 11)] + [(NX // 2, NZ // 2, 2)]
+        srcs = [poe.source(NX // 3 + 17 * s, npml + 4 + 5 * s, poe.SRC_RICKER_FZ if s == 0 else poe.SRC_REF_DGAUSS_P,
+                           f0, 1e3 if s == 0 else 1.0, 0.0 if s == 0 else 0.4) for s in range(nshots)]
+        out.append((g, coef, px, pz, srcs, rec))
+    return out
+
+
+def _solver(poe, case, fast):
+    g, coef, px, pz, srcs, rec = case
+    s = poe.Solver(g, coef, px, pz, fast=fast)
+    for src in srcs:
+        s.add_shot(src, rec)
+    return s
+
+
+def _state(s, nshots):
+    return [(s.traces(k), s.field("vz", k), s.field("p", k), s.field("wx", k), s.steps(k)) for k in range(nshots)]
+
+
+def _same(a, b):
+    for (ta, *fa, na), (tb, *fb, nb) in zip(a, b):
+        assert na == nb
+        assert np.array_equal(ta.view(np.uint32), tb.view(np.uint32))
+        for x, y in zip(fa, fb):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_batch_matches_single_runs(poe, fast):
+    cases = _build(poe, fast)
+    runs = [[150, 70, 0, 213, 64], [40, 0, 100, 64, 1]]     # uneven, with idle models and graph + tail segments
+    ref = [_solver(poe, c, fast) for c in cases]
+    for r in runs:
+        for i, s in enumerate(ref):
+            if r[i]:
+                s.run(r[i])
+    want = [_state(s, len(c[4])) for s, c in zip(ref, cases)]
+    for s in ref:
+        s.close()
+
+    solvers = [_solver(poe, c, fast) for c in cases]
+    with poe.Batch(solvers) as b:
+        for r in runs:
+            b.run(r)
+        b.sync()
+        assert b.launches > 0
+    for s, c, w in zip(solvers, cases, want):
+        _same(_state(s, len(c[4])), w)
+    # a solver keeps running on its own after the batch
+    solvers[1].run(33)
+    assert solvers[1].steps() == 70 + 33
+    for s in solvers:
+        s.close()
+
+
+def test_batch_rejects_mixed_contexts(poe):
+    cases = _build(poe, False)[:2]
+    a = _solver(poe, cases[0], False)
+    b = _solver(poe, cases[1], True)
+    with pytest.raises(poe.PoeError):
+        poe.Batch([a, b])                     # mixed stencil modes
+    g, coef, px, pz, srcs, rec = cases[1]
+    c = poe.Solver(g, coef, px, pz, palette=False)
+    c.add_shot(srcs[0], rec)
+    with pytest.raises(poe.PoeError):
+        poe.Batch([a, c])                     # coefficient-plane model
+    with pytest.raises(poe.PoeError):
+        poe.Batch([a, a])                     # listed twice
+    with poe.Batch([a]) as bt:
+        with pytest.raises(poe.PoeError):
+            bt.run([-1])
+    for s in (a, b, c):
+        s.close()
