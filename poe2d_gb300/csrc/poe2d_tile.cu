@@ -378,43 +378,99 @@ k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
 // material id and every per-cell coefficient the reference computes (co, c1,
 // c2, rhof*eta/kappa, 1/co, 1/c1) comes from a table row in shared memory.
 //
-// Persistent and double-buffered: one CTA of 512 threads per SM walks the
-// (shot, tile) list.  While it computes tile j from one shared-memory buffer,
-// TMA fills the other with tile j+1 (4 velocity planes + 5 state planes with
-// halos, one batch on an mbarrier) and cp.async brings its material ids, so
-// HBM traffic overlaps compute.  Threads form a 64 x 8 grid: a warp works 32
-// consecutive columns of one row (conflict-free shared-memory access).
+// Persistent, warp-specialised and double-buffered: one CTA per SM walks the
+// work list of (model, shot, tile) items.  A producer warp runs one item
+// ahead: it resolves the item's model and shot (a chain of dependent global
+// loads that would otherwise stall every warp at each item), writes the
+// item's parameters to shared memory, and fills the free buffer: TMA for the
+// 4 velocity and 5 state planes with halos, cp.async for the material ids,
+// the C-PML profile slices and the material table.  Sixteen compute warps
+// (a 64 x 8 thread grid; a warp works 32 consecutive columns of one row, so
+// shared-memory accesses are conflict-free) compute the item from the other
+// buffer.  Buffers are handed over with mbarriers (full: producer -> compute,
+// empty: compute -> producer); every wait is bounded.
 namespace {
-constexpr int PNT = 512;
+constexpr int PCT = 512;                           // compute threads
+constexpr int PNT = PCT + 32;                      // + the producer warp
 constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
-constexpr int QSW = QX + 4, QSH = QZ + 4;          // stress cells 64 x 36
+constexpr int QSH = QZ + 4;                         // stress rows: 64 x 36 cells
 constexpr int IW = TMA_VW, IH = QZ + 5;            // ids: cols x0-4 .. x0+63, rows z0-2 .. z0+34
 constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
 constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
 constexpr int PS_FLOATS = (PS_BOX + 31) / 32 * 32; // slot stride: 128-B aligned TMA destinations
+constexpr int PXW = TMA_VW, PZH = TMA_VH;          // profile slices: x0-4 .. x0+63, z0-4 .. z0+35
 constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
 constexpr int BUF_OFF_I = BUF_OFF_S + 5 * PS_FLOATS * 4;
-constexpr int BUF_BYTES = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
-constexpr int PAL_OFF_T = 2 * BUF_BYTES;
-constexpr int PAL_OFF_B = PAL_OFF_T + MAX_PALETTE * MT_W * 4;
-constexpr size_t PAL_SMEM = PAL_OFF_B + 16;
+constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
+constexpr int BUF_OFF_PZ = BUF_OFF_PX + 6 * PXW * 4;
+constexpr int BUF_OFF_T = BUF_OFF_PZ + 6 * PZH * 4;
+constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
+constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
+constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
+constexpr int PAL_OFF_B = 2 * BUF_BYTES;
+constexpr size_t PAL_SMEM = PAL_OFF_B + 64;
 constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4;
 static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
 static_assert((PV_FLOATS * 4) % 128 == 0 && (PS_FLOATS * 4) % 128 == 0, "TMA smem alignment");
-static_assert(IW % 4 == 0 && PAL_SMEM <= 232448, "shared memory budget");
+static_assert(BUF_OFF_PX % 16 == 0 && BUF_OFF_PZ % 16 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
+              "cp.async destinations");
+static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 4 == 0 && PAL_SMEM <= 232448, "shared memory budget");
 // state slots in shared memory; after the stress phase they hold its outputs
 enum { PS_G11 = 0, PS_G22, PS_XI1, PS_XI2, PS_SXZ };
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
+
+// what the producer resolves for one item (shared memory, per buffer)
+struct ItemMeta {
+    float *FB;                 // state buffer written by this step
+    const float *mxr, *mzr;    // stress C-PML memory read / written by this step
+    float *mxw, *mzw;
+    float *mxv, *mzv;          // velocity C-PML memory (in place)
+    float *acc_w;              // sigma2 at the source cell, written
+    float *trace_row;          // this step's trace row, or null
+    const int4 *rec;           // receivers of this tile
+    int nrec_q;
+    int src_off, src_where, src_on;
+    float src_val, pacc;
+    int x0, z0, interior;
+};
+static_assert(sizeof(ItemMeta) <= 128, "item parameters fit their slot");
 
 __device__ __forceinline__ void cp_async4(void *dst, const void *src)
 {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// the mbarrier's current phase also waits for this thread's earlier cp.async copies
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 // orders this thread's generic-proxy shared-memory accesses before later
 // async-proxy (TMA) writes to the same buffer
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// barrier of the 16 compute warps only
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(PCT) : "memory"); }
+// the same barrier, returning whether v held in every compute thread
+__device__ __forceinline__ bool compute_sync_and(bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(PCT)
+        : "memory");
+    return r != 0;
+}
 }  // namespace
 
 template <bool EXACT, bool KONE, bool MULTI>
@@ -423,94 +479,152 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
            const int4 *__restrict__ items, int nitems, int k)
 {
     extern __shared__ __align__(128) unsigned char smp[];
-    float *st = reinterpret_cast<float *>(smp + PAL_OFF_T);     // nmat x MT_W
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
+    uint64_t *empty = full + 2;
     const int tid = threadIdx.x;
-    const int lx = tid & 63, ly = tid >> 6;                      // 64 x 8 thread grid
-
-    // fill buffer b with work item w = (model, shot, x0, z0): thread 0 issues
-    // the TMA batch, everyone issues cp.async for the ids
-    auto issue = [&](int w, int b) {
-        const int4 it = items[w];
-        const ModelDev &m = MULTI ? models[it.x] : mp;
-        const StreamShot &S = shots[it.y];
-        const int x0 = it.z, z0 = it.w;
-        const int P = m.P;
-        unsigned char *buf = smp + b * BUF_BYTES;
-        if (tid == 0) {
-            const int64_t n = *S.step + k + 1;
-            const int cv = (int)((n - 1) & 1) * NSF;
-            float *sv = reinterpret_cast<float *>(buf);
-            float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
-            mbar_expect_tx(&bar[b], PAL_TX_BYTES);
-            for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, &bar[b]);
-            tma_load_3d(ss + PS_G11 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G11, &bar[b]);
-            tma_load_3d(ss + PS_G22 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G22, &bar[b]);
-            tma_load_3d(ss + PS_XI1 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI1, &bar[b]);
-            tma_load_3d(ss + PS_XI2 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI2, &bar[b]);
-            tma_load_3d(ss + PS_SXZ * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_SXZ, &bar[b]);
-        }
-        // ids: rows z0-2 .. z0+34, columns x0-4 .. x0+63 (4-byte aligned: x0 % 4 == 0)
-        const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
-        unsigned char *dst = buf + BUF_OFF_I;
-        for (int i = tid; i < IH * (IW / 4); i += PNT) {
-            const int r = i / (IW / 4), c = i - r * (IW / 4);
-            cp_async4(dst + 4 * i, src + (int64_t)r * P + 4 * c);
-        }
-        cp_async_commit();
-    };
 
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], PCT / 32);
+        }
         mbar_fence_init();
     }
-    int table_of = -1;                     // model whose material table is in shared memory
-    if (!MULTI) {
-        for (int i = tid; i < mp.nmat * MT_W; i += PNT) st[i] = mp.mtab[i];
-        table_of = 0;
-    }
     __syncthreads();
-    int w = blockIdx.x;
-    if (w < nitems) issue(w, 0);
 
-    for (int j = 0; w < nitems; ++j, w += gridDim.x) {
-        const int b = j & 1;
-        const int4 it = items[w];
-        const ModelDev &m = MULTI ? models[it.x] : mp;
-        if (MULTI && it.x != table_of) {   // the previous item's compute is over (trailing barrier)
-            for (int i = tid; i < m.nmat * MT_W; i += PNT) st[i] = m.mtab[i];
-            table_of = it.x;
+    // ------------------------------------------------------------ producer
+    if (tid >= PCT) {
+        const int lane = tid - PCT;
+        int j = 0;
+        for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
+            const int b = j & 1;
+            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
+                if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
+                break;
+            }
+            unsigned char *buf = smp + b * BUF_BYTES;
+            const int4 it = items[w];
+            const ModelDev &m = MULTI ? models[it.x] : mp;
+            const StreamShot &S = shots[it.y];
+            const int x0 = it.z, z0 = it.w;
+            const int P = m.P;
+            // ids, profile slices and the material table: cp.async, tracked by full[b]
+            {
+                const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
+                unsigned char *dst = buf + BUF_OFF_I;
+                for (int i = lane; i < IH * (IW / 4); i += 32) {
+                    const int r = i / (IW / 4), c = i - r * (IW / 4);
+                    cp_async4(dst + 4 * i, src + (int64_t)r * P + 4 * c);
+                }
+                float *px = reinterpret_cast<float *>(buf + BUF_OFF_PX);
+                float *pz = reinterpret_cast<float *>(buf + BUF_OFF_PZ);
+                for (int i = lane; i < 6 * (PXW / 4); i += 32) {
+                    const int r = i / (PXW / 4), c = i - r * (PXW / 4);
+                    cp_async16(px + r * PXW + 4 * c, m.px + (int64_t)r * P + x0 + 4 * c);
+                }
+                for (int i = lane; i < 6 * (PZH / 4); i += 32) {
+                    const int r = i / (PZH / 4), c = i - r * (PZH / 4);
+                    cp_async16(pz + r * PZH + 4 * c, m.pz + (int64_t)r * m.R + z0 + 4 * c);
+                }
+                if (MULTI) {
+                    float *t = reinterpret_cast<float *>(buf + BUF_OFF_T);
+                    for (int i = lane; i < m.nmat * (MT_W / 4); i += 32) cp_async16(t + 4 * i, m.mtab + 4 * i);
+                    // the model descriptor itself, for the compute warps
+                    const uint32_t *msrc = reinterpret_cast<const uint32_t *>(&m);
+                    uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
+                    for (int i = lane; i < (int)(sizeof(ModelDev) / 4); i += 32) mdst[i] = msrc[i];
+                }
+                cp_async_mbar_arrive(&full[b]);
+            }
+            // every lane's cp.async tracking is on full[b] before lane 0's arrival can complete the phase
+            __syncwarp();
+            if (lane == 0) {
+                const int64_t n = *S.step + k + 1;
+                const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+                ItemMeta &M = *reinterpret_cast<ItemMeta *>(buf + BUF_OFF_M);
+                M.FB = S.f[wr];
+                M.mxr = S.mx[rd];
+                M.mxw = S.mx[wr];
+                M.mzr = S.mz[rd];
+                M.mzw = S.mz[wr];
+                M.mxv = S.mxv;
+                M.mzv = S.mzv;
+                M.acc_w = S.acc + wr;
+                M.pacc = S.acc[rd];
+                M.src_off = (int)S.src_off;
+                M.src_where = S.src_where;
+                M.src_on = n <= S.src_n;
+                M.src_val = n <= S.src_n ? S.src_tab[n - 1] : 0.0f;
+                const bool rec_on = S.nrec > 0 && n <= S.trace_cap;
+                const int tile = (z0 / QZ) * m.ntx + x0 / QX;
+                const int qb = rec_on ? S.rec_start[tile] : 0, qe = rec_on ? S.rec_start[tile + 1] : 0;
+                M.rec = S.rec_sorted + qb;
+                M.nrec_q = qe - qb;
+                M.trace_row = rec_on ? S.trace + (n - 1) * S.nrec : nullptr;
+                M.x0 = x0;
+                M.z0 = z0;
+                // interior: no grid edge, C-PML strip or source within the tile and its halo
+                int sx = -1000000, sz = -1000000;
+                if (S.src_off >= 0) {
+                    sz = (int)(S.src_off / P) - ZH;
+                    sx = (int)(S.src_off - (int64_t)(sz + ZH) * P) - XH;
+                }
+                const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
+                M.interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
+                             zb <= m.NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
+                // the 4 velocity planes with a 4-cell halo and the 5 state planes with a 2-row halo
+                const int cv = rd * NSF;
+                float *sv = reinterpret_cast<float *>(buf);
+                float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
+                mbar_expect_tx(&full[b], PAL_TX_BYTES);
+                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, &full[b]);
+                tma_load_3d(ss + PS_G11 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
+                tma_load_3d(ss + PS_G22 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
+                tma_load_3d(ss + PS_XI1 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
+                tma_load_3d(ss + PS_XI2 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
+                tma_load_3d(ss + PS_SXZ * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+            }
+            __syncwarp();
         }
-        const bool ok = mbar_wait(&bar[b], (uint32_t)((j >> 1) & 1));
-        cp_async_wait_all();
-        if (!__syncthreads_and(ok)) {     // a bounded wait gave up: report, drain, leave
-            if (tid == 0) atomicExch(m.err, 1);
-            if (w + (int)gridDim.x < nitems) mbar_wait(&bar[b ^ 1], (uint32_t)(((j + 1) >> 1) & 1));
+        // copies in flight land before the CTA may exit: the last two fills
+        for (int i = j - 2 < 0 ? 0 : j - 2; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
+        return;
+    }
+
+    // ------------------------------------------------------------ compute
+    const int lx = tid & 63, ly = tid >> 6;        // 64 x 8 thread grid
+    if (!MULTI) {
+        // single model: one material table for every item, in buffer 0's slot
+        float *t0 = reinterpret_cast<float *>(smp + BUF_OFF_T);
+        for (int i = tid; i < mp.nmat * MT_W; i += PCT) t0[i] = mp.mtab[i];
+        compute_sync();
+    }
+    int j = 0;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
+        const int b = j & 1;
+        unsigned char *buf = smp + b * BUF_BYTES;
+        // a bounded wait that gave up in any compute thread ends all of them together
+        if (!compute_sync_and(mbar_wait(&full[b], (uint32_t)((j >> 1) & 1)))) {
+            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
             return;
         }
-        if (w + (int)gridDim.x < nitems) issue(w + gridDim.x, b ^ 1);   // buffer b^1 is free: item j-1 done
-
+        const ModelDev &m = MULTI ? *reinterpret_cast<const ModelDev *>(buf + BUF_OFF_MD) : mp;
+        const ItemMeta &IM = *reinterpret_cast<const ItemMeta *>(buf + BUF_OFF_M);
+        const float *st = reinterpret_cast<const float *>(MULTI ? buf + BUF_OFF_T : smp + BUF_OFF_T);
+        const float *PXs = reinterpret_cast<const float *>(buf + BUF_OFF_PX);
+        const float *PZs = reinterpret_cast<const float *>(buf + BUF_OFF_PZ);
         const int NX = m.NX, NZ = m.NZ;
         const int P = m.P;
         const int64_t PL = m.plane;
         const float dt = m.dt;
-        const float *__restrict__ PX = m.px;
-        const float *__restrict__ PZ = m.pz;
-        const int R = m.R;
         const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
-        const StreamShot &S = shots[it.y];
-        const int64_t n = *S.step + k + 1;
-        const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
-        const int x0 = it.z, z0 = it.w;
-        const int tile = (z0 / QZ) * m.ntx + x0 / QX;
-        float *__restrict__ FB = S.f[wr];
-        const int src_off = (int)S.src_off;
-        const int src_where = S.src_where;
-        const bool src_on = n <= S.src_n;
-        const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
-        const float pacc = S.acc[rd];
-        unsigned char *buf = smp + b * BUF_BYTES;
+        const int x0 = IM.x0, z0 = IM.z0;
+        float *__restrict__ FB = IM.FB;
+        const int src_off = IM.src_off;
+        const int src_where = IM.src_where;
+        const bool src_on = IM.src_on != 0;
+        const float src_val = IM.src_val;
+        const float pacc = IM.pacc;
         float *sv = reinterpret_cast<float *>(buf);                 // 4 x 40 x 68, from (x0-4, z0-4)
         float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);     // 5 x 36 x 68, from (x0-4, z0-2)
         const uint8_t *si = buf + BUF_OFF_I;                         // 37 x 68,     from (x0-4, z0-2)
@@ -528,13 +642,15 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 const bool x_own = x_ok && lx >= 2 && lx < QX + 2;
                 const int xc = (!IN && x_ok) ? xcol(m, x) : -1;
                 const int xi = x + XH;
-                const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-                const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-                const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-                const float Kx = KONE ? 1.0f : PX[PK * P + xi];
+                const int pxo = lx + 2;                          // x in the profile slice
+                const float bxh = PXs[PBH * PXW + pxo], axh = PXs[PAH * PXW + pxo];
+                const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
+                const float Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
+                const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo];
 #pragma unroll kPalStressUnroll
                 for (int zl = ly; zl < QSH; zl += 8) {
                     const int z = z0 - 2 + zl;
+                    const int pzo = zl + 2;                      // z in the profile slice
                     const int vo = (zl + 2) * TMA_VW + lx + 2;      // in the velocity tile
                     const int so = zl * TMA_VW + lx + 2;            // in the state tile
                     const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
@@ -559,34 +675,33 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float mu_top = st[MT_W * si[(zl + 1) * IW + lx + 2] + MT_MU];   // rmu[top] (cu:218)
                     const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
                     const int zr = (!IN && z_ok) ? zrow(m, z) : -1;
-                    const int zi = z + ZH;
                     float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
                     if (xc >= 0 && (g1 || g2)) {
                         const int ix = z * Wx + xc;
-                        const float *MA = S.mx[rd];
+                        const float *MA = IM.mxr;
                         m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
                         m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
                         m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
                         if (own) {
-                            float *MB = S.mx[wr];
+                            float *MB = IM.mxw;
                             if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
                             if (g2) MB[MXS_SXZ * nzx + ix] = m5;
                         }
                     }
                     if (zr >= 0 && (g1 || g2)) {
                         const int iz = zr * P + xi;
-                        const float *MA = S.mz[rd];
-                        const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
+                        const float *MA = IM.mzr;
+                        const float bz = PZs[PB * PZH + pzo], az = PZs[PA * PZH + pzo];
                         m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
                         m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-                        m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
+                        m6 = PZs[PBH * PZH + pzo] * MA[MZS_SXZ * hzp + iz] + PZs[PAH * PZH + pzo] * sdz;
                         if (own) {
-                            float *MB = S.mz[wr];
+                            float *MB = IM.mzw;
                             if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
                             if (g2) MB[MZS_SXZ * hzp + iz] = m6;
                         }
                     }
-                    const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
+                    const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo];
                     if (g1) {   // cu:71-86
                         g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
                         g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
@@ -597,7 +712,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const bool is_src = !IN && cell_ok && o == src_off;
                     if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
                     if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-                    if (is_src && own) S.acc[wr] = pv;
+                    if (is_src && own) *IM.acc_w = pv;
                     if (g2) {   // cu:223-226
                         const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
                         sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
@@ -621,14 +736,13 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ss[PO_SXZ * PS_FLOATS + so] = sxz;
                 }
             }
-            __syncthreads();
+            compute_sync();
 
             // ---- receivers of this tile (vx, vz before the update; p of this step)
-            if (S.nrec > 0 && n <= S.trace_cap) {
-                const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
-                float *trace_row = S.trace + (n - 1) * S.nrec;
-                for (int q = qb + tid; q < qe; q += PNT) {
-                    const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
+            if (IM.nrec_q > 0) {
+                float *trace_row = IM.trace_row;
+                for (int q = tid; q < IM.nrec_q; q += PCT) {
+                    const int4 Rq = IM.rec[q];                   // (x, comp, slot, z)
                     const int xl = Rq.x - x0, zl = Rq.w - z0;
                     float v;
                     if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
@@ -639,20 +753,22 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
 
             // ---- velocity on the tile: column lx (< 60), rows ly, ly+8, ...
             if (lx < QX) {
-                float *__restrict__ MXV = S.mxv;
-                float *__restrict__ MZV = S.mzv;
+                float *__restrict__ MXV = IM.mxv;
+                float *__restrict__ MZV = IM.mzv;
                 const int x = x0 + lx;
                 const bool x_in = IN || x <= NX;
                 const bool x_vx = IN || (x >= 2 && x <= NX - 1), x_vz = IN || (x >= 1 && x <= NX - 2);   // cu:289, 326
                 const int xc = (!IN && x_in) ? xcol(m, x) : -1;
                 const int xi = x + XH;
-                const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-                const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-                const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
+                const int pxo = lx + 4;
+                const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
+                const float bxh = PXs[PBH * PXW + pxo], axh = PXs[PAH * PXW + pxo];
+                const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo], Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
 #pragma unroll kPalVelUnroll
                 for (int zl = ly; zl < QZ; zl += 8) {
                     const int t = z0 + zl;
                     if (!IN && (!x_in || t > NZ)) continue;
+                    const int pzo = zl + 4;
                     const int so = (zl + 2) * TMA_VW + lx + 4;      // (x, t) in the stress tile
                     const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
                     const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
@@ -660,7 +776,6 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
                     const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
                     const int o = (t + ZH) * P + xi;
-                    const int zi = t + ZH;
                     const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
                     const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
                     const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
@@ -685,14 +800,14 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         const int iz = zr * P + xi;
                         float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
                         float *M6 = MZV + MZV_VZ2 * hzp + iz;
-                        const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
-                        m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
+                        const float bh = PZs[PBH * PZH + pzo], ah = PZs[PAH * PZH + pzo];
+                        m3 = PZs[PB * PZH + pzo] * *M3 + PZs[PA * PZH + pzo] * d3x;
                         m5 = bh * *M5 + ah * d2z;
                         m6 = bh * *M6 + ah * d3z;
                         if (gvx) *M3 = m3;
                         if (gvz) { *M5 = m5; *M6 = m6; }
                     }
-                    const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
+                    const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo], Kzh = KONE ? 1.0f : PZs[PKH * PZH + pzo];
                     float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
                     {   // vx, wx, material at (x, t) (cu:293-311)
                         const float *mt = st + MT_W * si[(zl + 2) * IW + lx + 4];
@@ -724,17 +839,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 }
             }
         };
-        {
-            int sx = -1000000, sz = -1000000;
-            if (src_off >= 0) { sz = src_off / P - ZH; sx = src_off - (sz + ZH) * P - XH; }
-            const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
-            const bool interior = xa >= 2 && xa >= m.xL && xb <= NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
-                                  zb <= NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
-            if (interior) compute(std::true_type{});
-            else compute(std::false_type{});
-        }
+        if (IM.interior) compute(std::true_type{});
+        else compute(std::false_type{});
+        // hand buffer b back to the producer
         fence_proxy_async();
-        __syncthreads();   // buffer b is reissued by the next item's prefetch
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&empty[b]);
     }
 }
 

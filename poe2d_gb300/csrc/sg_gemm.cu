@@ -1,0 +1,293 @@
+// sg_gemm.cu -- BF16 tensor-core GEMM for the surrogate network (sm_103a).
+//
+//   C[M x N] = alpha * A[M x K] . B[N x K]^T (+ bias[n]) (ReLU) (+= C)
+//
+// A and B are bf16, row-major with K contiguous (K-major), FP32 accumulation
+// in tensor memory.  One CTA of 128 threads computes a 128 x BN tile:
+//   thread 0    TMA producer: a 4-stage ring of 128x64 (A) and BNx64 (B)
+//               tiles, 128-byte swizzled, one mbarrier per stage;
+//   thread 32   MMA issuer: four tcgen05.mma (K = 16 each) per stage, then
+//               tcgen05.commit frees the stage; a last commit signals the end;
+//   warps 0-3   epilogue: each warp reads its 32 TMEM lanes (rows) with
+//               tcgen05.ld and applies alpha, bias, ReLU, the bf16/f32 stores.
+// K may be split over blockIdx.z (ksplit > 1): each split writes an FP32
+// partial tile to a workspace and a reduction kernel applies the epilogue in
+// a fixed order, so results do not depend on scheduling.
+//
+// Out-of-range rows and K columns of a TMA box are zero-filled by the copy
+// engine, so M, N and K need no padding; the global row pitches must be
+// multiples of 8 elements (16 bytes) and the bases 16-byte aligned.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "sg_internal.h"
+#include "sm103_ptx.cuh"
+
+namespace sg {
+using namespace sm103;
+
+namespace {
+constexpr int BM = 128, BK = 64, STAGES = 4, NT = 128;
+
+template <int BN>
+struct GemmSmem {
+    static constexpr int A_BYTES = BM * BK * 2;             // 16 KB
+    static constexpr int B_BYTES = BN * BK * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int BAR_OFF = STAGES * STAGE;
+    static constexpr int TOTAL = BAR_OFF + (2 * STAGES + 1) * 8 + 8 + 1024;   // + alignment slack
+    static constexpr uint32_t TX = (uint32_t)STAGE;
+    static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(NT, 1)
+k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int M, int N, int K,
+       int kblocks_per_split, Epilogue e, float *partial, int *err)
+{
+    using L = GemmSmem<BN>;
+    extern __shared__ unsigned char smraw[];
+    unsigned char *sm = (unsigned char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + L::BAR_OFF);
+    uint64_t *empty = full + STAGES;
+    uint64_t *done = empty + STAGES;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int nkb_total = (K + BK - 1) / BK;
+    const int kb0 = blockIdx.z * kblocks_per_split;
+    int kb1 = kb0 + kblocks_per_split;
+    if (kb1 > nkb_total) kb1 = nkb_total;
+    const int nkb = kb1 > kb0 ? kb1 - kb0 : 0;
+
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        mbar_fence_init();
+    }
+    if (warp == 2) tmem_alloc(tslot, L::TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    bool ok = true;
+
+    if (tid == 0) {   // producer
+        int issued = 0;
+        for (int i = 0; i < nkb; ++i) {
+            const int s = i % STAGES;
+            if (i >= STAGES && !mbar_wait(&empty[s], (uint32_t)(((i / STAGES) - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            unsigned char *a = sm + s * L::STAGE;
+            mbar_expect_tx(&full[s], L::TX);
+            tma_load_2d(a, &tA, (kb0 + i) * BK, m0, &full[s]);
+            tma_load_2d(a + L::A_BYTES, &tB, (kb0 + i) * BK, n0, &full[s]);
+            issued = i + 1;
+        }
+        // copies still in flight must land before the CTA can leave
+        for (int i = issued - STAGES < 0 ? 0 : issued - STAGES; i < issued; ++i)
+            if (!mbar_wait(&full[i % STAGES], (uint32_t)((i / STAGES) & 1))) ok = false;
+    } else if (tid == 32) {   // MMA issuer
+        constexpr uint32_t idesc = idesc_bf16_f32(BM, BN);
+        for (int i = 0; i < nkb; ++i) {
+            const int s = i % STAGES;
+            if (!mbar_wait(&full[s], (uint32_t)((i / STAGES) & 1))) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(sm + s * L::STAGE);
+            const uint64_t ad = desc_k_sw128(a), bd = desc_k_sw128(a + L::A_BYTES);
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k)
+                tc_mma_f16(tmem, ad + 2 * k, bd + 2 * k, idesc, (i | k) ? 1u : 0u);
+            tc_commit(&empty[s]);
+        }
+        tc_commit(done);   // arrives once every MMA above has completed
+    }
+    __syncwarp();
+
+    // epilogue: warp w owns TMEM lanes (tile rows) 32w .. 32w+31
+    if (!mbar_wait(done, 0)) ok = false;
+    tc_fence_after();
+    if (!ok) atomicExch(err, 1);
+    const int row = m0 + warp * 32 + lane;
+    const bool row_ok = row < M && nkb > 0;
+#pragma unroll 1
+    for (int c = 0; c < BN / 16; ++c) {
+        uint32_t v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+        tmem_ld_wait();
+        if (!row_ok || !ok) continue;
+        const int nb = n0 + c * 16;
+        if (partial) {   // split-K: raw partial sums
+            float *p = partial + ((size_t)blockIdx.z * M + row) * e.ldc + nb;
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (nb + j < N) p[j] = __uint_as_float(v[j]);
+            continue;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int n = nb + j;
+            if (n >= N) continue;
+            float x = e.alpha * __uint_as_float(v[j]);
+            if (e.bias) x += e.bias[n];
+            if (e.relu) x = fmaxf(x, 0.0f);
+            const size_t o = (size_t)row * e.ldc + n;
+            if (e.out_f32) {
+                if (e.accumulate) x += e.out_f32[o];
+                e.out_f32[o] = x;
+            }
+            if (e.out_bf16) e.out_bf16[o] = __float2bfloat16_rn(x);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) tmem_dealloc(tmem, L::TMEM_COLS);
+}
+
+// sum of the split-K partials in split order, then the epilogue
+__global__ void k_splitk_reduce(const float *partial, int splits, int M, int N, Epilogue e)
+{
+    const size_t total = (size_t)M * N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int row = (int)(i / N), n = (int)(i - (size_t)row * N);
+        const size_t o = (size_t)row * e.ldc + n;
+        float x = 0.0f;
+        for (int s = 0; s < splits; ++s) x += partial[(size_t)s * M * e.ldc + o];
+        x *= e.alpha;
+        if (e.bias) x += e.bias[n];
+        if (e.relu) x = fmaxf(x, 0.0f);
+        if (e.out_f32) {
+            if (e.accumulate) x += e.out_f32[o];
+            e.out_f32[o] = x;
+        }
+        if (e.out_bf16) e.out_bf16[o] = __float2bfloat16_rn(x);
+    }
+}
+
+typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                             const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                             CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn()
+{
+    static EncodeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeFn)p;
+    });
+    return fn;
+}
+
+// bf16 rows x cols (cols contiguous, pitch ld elements), box 64 x box_rows, 128-B swizzle
+bool make_map(CUtensorMap *m, const void *base, int rows, int cols, int ld, int box_rows)
+{
+    EncodeFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int sm_count()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+template <int BN>
+int launch(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, int splits, int kper, const Epilogue &e,
+           float *ws, int *err, cudaStream_t st)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmSmem<BN>::TOTAL);
+        attr = true;
+    }
+    const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
+    k_gemm<BN><<<grid, NT, GemmSmem<BN>::TOTAL, st>>>(ta, tb, M, N, K, kper, e, splits > 1 ? ws : nullptr, err);
+    return (int)cudaGetLastError();
+}
+}  // namespace
+
+int gemm(const Gemm &g, const Epilogue &e, float *ws, int64_t ws_floats, int *err, cudaStream_t st)
+{
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) return (int)cudaErrorInvalidValue;
+    if (g.lda % 8 || g.ldb % 8 || g.lda < g.K || g.ldb < g.K || ((uintptr_t)g.A & 15) || ((uintptr_t)g.B & 15))
+        return (int)cudaErrorInvalidValue;
+    if (e.ldc < g.N) return (int)cudaErrorInvalidValue;
+    const int BN = g.N > 64 ? 128 : 64;
+    CUtensorMap ta, tb;
+    if (!make_map(&ta, g.A, g.M, g.K, g.lda, BM) || !make_map(&tb, g.B, g.N, g.K, g.ldb, BN))
+        return (int)cudaErrorInvalidValue;
+    // split K when the tile grid leaves most SMs idle and K is long
+    const int tiles = ((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN);
+    const int nkb = (g.K + BK - 1) / BK;
+    int splits = 1;
+    if (ws && tiles < sm_count() / 2 && nkb >= 8) {
+        splits = sm_count() / tiles;
+        if (splits > kMaxSplits) splits = kMaxSplits;
+        if (splits > nkb / 4) splits = nkb / 4;
+        if (splits < 1) splits = 1;
+        while (splits > 1 && (int64_t)splits * g.M * e.ldc > ws_floats) --splits;
+    }
+    const int kper = (nkb + splits - 1) / splits;
+    splits = (nkb + kper - 1) / kper;
+    int rc = BN == 128 ? launch<128>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
+                       : launch<64>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st);
+    if (rc || splits == 1) return rc;
+    const int64_t total = (int64_t)g.M * g.N;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 4 * sm_count()) blocks = 4 * sm_count();
+    k_splitk_reduce<<<blocks, 256, 0, st>>>(ws, splits, g.M, g.N, e);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace sg
+
+// ---- C ABI: the GEMM on its own (device pointers), for tests and callers
+// that drive the tensor cores directly
+extern "C" int poe_sg_gemm(const void *A, int32_t lda, const void *B, int32_t ldb, int32_t M, int32_t N, int32_t K,
+                           float alpha, const float *bias, int32_t relu, float *out_f32, void *out_bf16, int32_t ldc,
+                           int32_t accumulate, float *ws, int64_t ws_floats, int32_t *err_dev, void *stream)
+{
+    if (!A || !B || !err_dev || (!out_f32 && !out_bf16)) return 1;   // POE_EINVAL
+    sg::Gemm g{static_cast<const __nv_bfloat16 *>(A), lda, static_cast<const __nv_bfloat16 *>(B), ldb, M, N, K};
+    sg::Epilogue e;
+    e.alpha = alpha;
+    e.bias = bias;
+    e.relu = relu;
+    e.out_f32 = out_f32;
+    e.out_bf16 = static_cast<__nv_bfloat16 *>(out_bf16);
+    e.ldc = ldc;
+    e.accumulate = accumulate;
+    const int rc = sg::gemm(g, e, ws, ws_floats, err_dev, (cudaStream_t)stream);
+    return rc == 0 ? 0 : (rc == (int)cudaErrorInvalidValue ? 1 : 5);   // POE_OK / POE_EINVAL / POE_ECUDA
+}

@@ -1,0 +1,35 @@
+// sg_internal.h -- device-side interfaces of the surrogate network kernels.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace sg {
+
+constexpr int kMaxSplits = 16;
+
+// C = alpha * A . B^T: A is M x K (pitch lda), B is N x K (pitch ldb), bf16, K contiguous
+struct Gemm {
+    const __nv_bfloat16 *A;
+    int lda;
+    const __nv_bfloat16 *B;
+    int ldb;
+    int M, N, K;
+};
+
+struct Epilogue {
+    float alpha = 1.0f;
+    const float *bias = nullptr;          // [N]
+    int relu = 0;
+    float *out_f32 = nullptr;             // [M x ldc]
+    __nv_bfloat16 *out_bf16 = nullptr;    // [M x ldc]
+    int ldc = 0;
+    int accumulate = 0;                   // out_f32 += result
+};
+
+// Launch on st; ws (may be null: no split-K) holds kMaxSplits * M * ldc floats.
+// Returns a cudaError_t value.  A bounded wait that gave up sets *err = 1.
+int gemm(const Gemm &g, const Epilogue &e, float *ws, int64_t ws_floats, int *err, cudaStream_t st);
+
+}  // namespace sg
