@@ -93,6 +93,22 @@ SYMBOLS = {
     "poe_batch_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "poe_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "poe_batch_destroy": (None, [C.c_void_p]),
+    "poe_sg_gemm": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                              C.c_float, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                              C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "poe_sg_create": (C.c_int, [C.c_int32, C.c_uint64, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "poe_sg_param_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "poe_sg_get_params": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
+    "poe_sg_set_params": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
+    "poe_sg_get_grads": (C.c_int, [C.c_void_p, _fp, C.c_int64]),
+    "poe_sg_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "poe_sg_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "poe_sg_adam": (C.c_int, [C.c_void_p, C.c_float]),
+    "poe_sg_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float,
+                                    C.POINTER(C.c_float)]),
+    "poe_sg_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "poe_sg_last_error": (C.c_char_p, [C.c_void_p]),
+    "poe_sg_destroy": (None, [C.c_void_p]),
     "poe_ref_receivers": (C.c_int32, [C.POINTER(Grid), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.POINTER(Receiver), C.c_int32]),
 }

@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, "libpoe2d.so")
 CLI = os.path.join(BUILD, "poe2d_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["poe2d_tile.cu", "poe2d_api.cpp", "poe2d_setup.cpp", "sg_gemm.cu"]
+SOURCES = ["poe2d_tile.cu", "poe2d_api.cpp", "poe2d_setup.cpp", "sg_gemm.cu", "sg_ops.cu", "sg_net.cpp"]
 
 
 def nvcc():

@@ -1,0 +1,88 @@
+"""Python face of the learned surrogate (include/poe2d_surrogate.h).
+
+``Surrogate`` wraps one network: parameters, inference, training steps.  The
+tensors it takes are torch CUDA tensors (device memory and streams come from
+torch; every kernel is the library's own).  ``Ensemble`` holds four members
+trained from different seeds; where their predictions disagree by more than a
+threshold the caller falls back to the solver.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import PoeError
+
+MAP, MAP_CH, SCALARS, SAMPLES, CHANNELS = 64, 2, 3, 1024, 384
+
+
+class Surrogate:
+    def __init__(self, max_batch=256, seed=0, stream=None):
+        h = C.c_void_p()
+        st = L.lib().poe_sg_create(int(max_batch), int(seed), C.c_void_p(stream or 0), C.byref(h))
+        if st != L.POE_OK:
+            raise PoeError(st, "poe_sg_create")
+        self.h = h
+        self.max_batch = max_batch
+        n = C.c_int64(0)
+        L.lib().poe_sg_param_count(self.h, C.byref(n))
+        self.nparam = n.value
+
+    def _check(self, st):
+        if st != L.POE_OK:
+            m = L.lib().poe_sg_last_error(self.h)
+            raise PoeError(st, m.decode() if m else "")
+
+    def close(self):
+        if getattr(self, "h", None):
+            L.lib().poe_sg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        out = np.empty(self.nparam, np.float32)
+        self._check(L.lib().poe_sg_get_params(self.h, out.ctypes.data_as(L._fp), self.nparam))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._check(L.lib().poe_sg_set_params(self.h, p.ctypes.data_as(L._fp), p.size))
+
+    def grads(self):
+        out = np.empty(self.nparam, np.float32)
+        self._check(L.lib().poe_sg_get_grads(self.h, out.ctypes.data_as(L._fp), self.nparam))
+        return out
+
+    def forward(self, maps, scalars, out=None):
+        """maps: bf16 [B, 64, 64, 2], scalars: f32 [B, 3] (CUDA) -> f32 [B, 1024, 384]."""
+        import torch
+        B = maps.shape[0]
+        if out is None:
+            out = torch.empty((B, SAMPLES, CHANNELS), dtype=torch.float32, device=maps.device)
+        self._check(L.lib().poe_sg_forward(self.h, maps.data_ptr(), scalars.data_ptr(), B, out.data_ptr()))
+        return out
+
+    def loss_grad(self, maps, scalars, targets):
+        loss = C.c_float(0.0)
+        self._check(L.lib().poe_sg_loss_grad(self.h, maps.data_ptr(), scalars.data_ptr(), targets.data_ptr(),
+                                             maps.shape[0], C.byref(loss)))
+        return loss.value
+
+    def adam(self, lr):
+        self._check(L.lib().poe_sg_adam(self.h, float(lr)))
+
+    def train_step(self, maps, scalars, targets, lr):
+        loss = C.c_float(0.0)
+        self._check(L.lib().poe_sg_train_step(self.h, maps.data_ptr(), scalars.data_ptr(), targets.data_ptr(),
+                                              maps.shape[0], float(lr), C.byref(loss)))
+        return loss.value
+
+    @property
+    def launches(self):
+        n = C.c_int64(0)
+        self._check(L.lib().poe_sg_launches(self.h, C.byref(n)))
+        return n.value

@@ -1,0 +1,77 @@
+"""The surrogate network on the tensor cores against its CPU reference
+(oracle/surrogate_ref.py, bf16 rounding emulated at the same points): the
+forward pass, the loss and every parameter gradient; plus determinism and a
+training run that must fit a fixed batch."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _batch(B, seed):
+    g = torch.Generator().manual_seed(seed)
+    maps = torch.rand((B, 64, 64, 2), generator=g)
+    sc = torch.rand((B, 3), generator=g)
+    tgt = 0.05 * torch.randn((B, 1024, 384), generator=g)
+    return maps, sc, tgt
+
+
+def _dev(maps, sc, tgt):
+    return (maps.to(torch.bfloat16).cuda(), sc.float().cuda(), tgt.to(torch.bfloat16).cuda())
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_forward_loss_and_gradients_match_reference(poe):
+    from oracle import surrogate_ref as R
+    from poe2d_gb300.surrogate import Surrogate
+    net = Surrogate(max_batch=16, seed=3)
+    assert net.nparam == R.param_count()
+    p = net.params()
+    maps, sc, tgt = _batch(8, 1)
+    dm, ds, dt = _dev(maps, sc, tgt)
+    out = net.forward(dm, ds).cpu().numpy()
+    mq = dm.float().cpu().numpy()
+    tq = dt.float().cpu().numpy()
+    ref = R.forward(p, mq, sc.numpy())
+    assert _rel(out, ref) <= 1e-2
+    loss = net.loss_grad(dm, ds, dt)
+    g = net.grads()
+    rloss, rg = R.loss_and_grads(p, mq, sc.numpy(), tq)
+    assert abs(loss - rloss) <= 1e-3 * rloss
+    q = 0
+    for i, (kind, ci, co, *_) in enumerate(R.LAYERS):
+        n = co * R._k(kind, ci) + co
+        a, b = g[q:q + n], rg[q:q + n]
+        cos = float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300))
+        assert _rel(a, b) <= 5e-2 and cos >= 0.998, (i, _rel(a, b), cos)
+        q += n
+    # deterministic: the same batch gives the same gradient bits
+    net.loss_grad(dm, ds, dt)
+    assert np.array_equal(net.grads().view(np.uint32), g.view(np.uint32))
+    net.close()
+
+
+def test_params_roundtrip_and_training_fits_a_batch(poe):
+    from poe2d_gb300.surrogate import Surrogate
+    net = Surrogate(max_batch=16, seed=5)
+    p = net.params()
+    net.set_params(p * 0.5)
+    assert np.array_equal(net.params(), (p * 0.5).astype(np.float32))
+    net.set_params(p)
+    maps, sc, _ = _batch(16, 2)
+    # targets the network can represent: another network's output
+    teacher = Surrogate(max_batch=16, seed=9)
+    dm, ds = maps.to(torch.bfloat16).cuda(), sc.float().cuda()
+    tgt = teacher.forward(dm, ds).to(torch.bfloat16)
+    l0 = net.loss_grad(dm, ds, tgt)
+    for _ in range(60):
+        loss = net.train_step(dm, ds, tgt, 1e-3)
+    assert loss < 0.2 * l0, (l0, loss)
+    assert net.launches > 0
+    net.close()
+    teacher.close()
