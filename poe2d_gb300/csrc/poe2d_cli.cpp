@@ -46,6 +46,7 @@ struct Opts {
     std::string medium = "mar_poro_2440x13600.bin", cp = "mar_cp_2440x13600.bin";   // cu:606, 616
     std::string cs = "mar_cs_2440x13600.bin", rho = "mar_rho_2440x13600.bin";       // cu:626, 636
     std::string fluid;                     // optional table file: rows of K_f eta kappa phi tortuosity rho_f
+    std::string checkpoint, restart;       // full-state image written at each snapshot / read at start
     char order = 'x';
     bool fast = false, dry = false, snapshots = true, medium_dump = true;
 };
@@ -74,6 +75,8 @@ void usage()
         "  --fast                 plain FP32 stencils (default: the reference's rounding)\n"
         "  --no-snapshots         skip the .vzo/.vxo files\n"
         "  --no-medium-dump       skip mediumrho.ctxt\n"
+        "  --checkpoint F         write the shot's full state to F at every snapshot (restartable)\n"
+        "  --restart F            continue from a --checkpoint image of the same run\n"
         "  --dry-run              read and check inputs, build coefficients and profiles, no GPU\n";
 }
 
@@ -100,6 +103,7 @@ bool parse(int argc, char **argv, Opts &o)
         INT_OPT("--panj", panj) INT_OPT("--panj2", panj2) INT_OPT("--samp", samp) INT_OPT("--npml", npml)
         STR_OPT("--medium", medium) STR_OPT("--cp", cp) STR_OPT("--cs", cs) STR_OPT("--rho", rho)
         STR_OPT("--fluid", fluid) STR_OPT("--in", in_dir) STR_OPT("--out", out_dir)
+        STR_OPT("--checkpoint", checkpoint) STR_OPT("--restart", restart)
         else if (a == "--order") {
             if (!(v = val("--order"))) return false;
             o.order = v[0];
@@ -295,14 +299,38 @@ int main(int argc, char **argv)
     int32_t shot = 0;
     if ((st = poe_add_shot(ctx, &src, rec.data(), nrec, &shot)) != POE_OK) return fail(ctx, st, "shot");
 
-    std::vector<float> snap(o.snapshots ? n : 0);
     int64_t done = 0;
+    if (!o.restart.empty()) {   // continue where a checkpointed run stopped
+        std::FILE *f = std::fopen(o.restart.c_str(), "rb");
+        if (!f) return fail(ctx, POE_EIO, o.restart.c_str());
+        std::vector<char> img;
+        char chunk[1 << 16];
+        size_t got;
+        while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) img.insert(img.end(), chunk, chunk + got);
+        std::fclose(f);
+        if ((st = poe_checkpoint_load(ctx, shot, img.data(), (int64_t)img.size())) != POE_OK)
+            return fail(ctx, st, "restart");
+        poe_steps_done(ctx, shot, &done);
+        if (done > nstep) return fail(ctx, POE_EINVAL, "checkpoint is past NSTEP");
+    }
+    std::vector<float> snap(o.snapshots ? n : 0);
     char name[128];
     while (done < nstep) {   // chunks of samp steps with their snapshots (cu:1620-1727)
-        const int64_t k = std::min<int64_t>(o.samp, nstep - done);
+        const int64_t k = std::min<int64_t>(o.samp - done % o.samp, nstep - done);
         if ((st = poe_run(ctx, k)) != POE_OK) return fail(ctx, st, "run");
         done += k;
-        if (k == o.samp && o.snapshots) {
+        if (done % o.samp == 0 && !o.checkpoint.empty()) {
+            int64_t bytes = 0;
+            poe_checkpoint_size(ctx, shot, &bytes);
+            std::vector<char> img((size_t)bytes);
+            if ((st = poe_checkpoint_save(ctx, shot, img.data(), bytes)) != POE_OK) return fail(ctx, st, "checkpoint");
+            const std::string tmp = o.checkpoint + ".tmp";
+            std::FILE *f = std::fopen(tmp.c_str(), "wb");
+            const bool w = f && std::fwrite(img.data(), 1, img.size(), f) == img.size();
+            if (f) std::fclose(f);
+            if (!w || std::rename(tmp.c_str(), o.checkpoint.c_str()) != 0) return fail(ctx, POE_EIO, "checkpoint file");
+        }
+        if (done % o.samp == 0 && o.snapshots) {
             std::snprintf(name, sizeof name, "vz%05i.vzo", (int)done);
             if ((st = poe_get_field(ctx, shot, POE_F_VZ, snap.data())) != POE_OK) return fail(ctx, st, "vz");
             if (!write_raw(path(o.out_dir, name), snap.data(), n)) return fail(ctx, POE_EIO, name);

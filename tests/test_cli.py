@@ -125,3 +125,21 @@ def test_cli_outputs_match_library_run(tmp_path, poe):
     for i, pat in enumerate(("recats%08d.ats", "recbwh%08d.bwh", "recsrc%08d.src")):
         with open(os.path.join(d, pat % int(f0))) as f:
             assert f.read() == "".join("%g " % float(v) for v in tr[:, 45 + i]), pat
+
+
+@pytest.mark.gpu
+def test_cli_restart_from_checkpoint_gives_the_same_files(tmp_path):
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    _write_case(str(a), nstep=150)
+    _write_case(str(b), nstep=150)
+    ck = str(tmp_path / "ck.img")
+    r = subprocess.run(_args(str(a), extra=["--checkpoint", ck]), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.getsize(ck) > 0                  # image of step 128
+    r = subprocess.run(_args(str(b), extra=["--restart", ck]), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for name in ("recvspvz00000200.vsp", "rechorvx00000200.hor", "recsrc00000200.src"):
+        assert (a / name).read_bytes() == (b / name).read_bytes(), name
+    assert not (b / "vz00064.vzo").exists()          # restarted past the first snapshot
