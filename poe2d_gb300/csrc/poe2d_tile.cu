@@ -41,14 +41,6 @@ constexpr int NT = 256;
 #endif
 constexpr int kStressUnroll = STRESS_UNROLL;   // cells in flight per thread (memory-level parallelism)
 constexpr int kVelUnroll = VEL_UNROLL;
-#ifndef PAL_SUNROLL
-#define PAL_SUNROLL 1
-#endif
-#ifndef PAL_VUNROLL
-#define PAL_VUNROLL 1
-#endif
-constexpr int kPalStressUnroll = PAL_SUNROLL;   // palette kernel: rows per thread interleaved
-constexpr int kPalVelUnroll = PAL_VUNROLL;
 constexpr int V_FLOATS = VW * VH, S_FLOATS = SW * SH;
 enum { SV_VX = 0, SV_VZ, SV_WX, SV_WZ };
 enum { SS_SXX = 0, SS_SZZ, SS_SXZ, SS_P };
@@ -384,16 +376,19 @@ k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
 // loads that would otherwise stall every warp at each item), writes the
 // item's parameters to shared memory, and fills the free buffer: TMA for the
 // 4 velocity and 5 state planes with halos, cp.async for the material ids,
-// the C-PML profile slices and the material table.  Sixteen compute warps
-// (a 64 x 8 thread grid; a warp works 32 consecutive columns of one row, so
-// shared-memory accesses are conflict-free) compute the item from the other
-// buffer.  Buffers are handed over with mbarriers (full: producer -> compute,
+// the C-PML profile slices and the material table.  Eighteen compute warps
+// compute the item from the other buffer: a warp works 32 consecutive
+// columns (conflict-free shared-memory rows) of a band of 4 consecutive rows,
+// so the z-stencils of a column reuse the values of the rows before them in
+// registers.  Stress: 9 bands x 2 halves cover the 64 x 36 stress cells;
+// velocity: 8 bands x 2 halves cover the 60 x 32 tile while the last two
+// warps record the tile's receivers.  Buffers are handed over with mbarriers (full: producer -> compute,
 // empty: compute -> producer); every wait is bounded.
 namespace {
-constexpr int PCT = 512;                           // compute threads
+constexpr int PCT = 576;                           // compute threads: 18 warps
+constexpr int ROWS = 4;                            // consecutive rows per compute thread
 constexpr int PNT = PCT + 32;                      // + the producer warp
 constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
-constexpr int QSH = QZ + 4;                         // stress rows: 64 x 36 cells
 constexpr int IW = TMA_VW, IH = QZ + 5;            // ids: cols x0-4 .. x0+63, rows z0-2 .. z0+34
 constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
 constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
@@ -434,6 +429,8 @@ struct ItemMeta {
     int x0, z0, interior;
 };
 static_assert(sizeof(ItemMeta) <= 128, "item parameters fit their slot");
+static_assert(PCT == 32 * 2 * ((QZ + 4) / ROWS) && (QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT / 32 > 2 * (QZ / ROWS),
+              "stress bands cover the 36 stress rows; velocity bands the 32 tile rows, with warps left for receivers");
 
 __device__ __forceinline__ void cp_async4(void *dst, const void *src)
 {
@@ -592,7 +589,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     }
 
     // ------------------------------------------------------------ compute
-    const int lx = tid & 63, ly = tid >> 6;        // 64 x 8 thread grid
+    const int wid = tid >> 5;
+    const int lx = (wid & 1) * 32 + (tid & 31);    // column in the 64-wide tile
+    const int zb0 = (wid >> 1) * ROWS;             // first row of this warp's band
     if (!MULTI) {
         // single model: one material table for every item, in buffer 0's slot
         float *t0 = reinterpret_cast<float *>(smp + BUF_OFF_T);
@@ -633,7 +632,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         // and its halo) take a copy of the code with every guard constant-true.
         auto compute = [&](auto interior_tag) {
             constexpr bool IN = decltype(interior_tag)::value;
-            // ---- stress on the tile + 2-cell halo: column lx, rows ly, ly+8, ...
+            // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
             {
                 const int x = x0 - 2 + lx;
                 const bool x_ok = IN || (x >= 0 && x <= NX);
@@ -647,14 +646,27 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
                 const float Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
                 const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo];
-#pragma unroll kPalStressUnroll
-                for (int zl = ly; zl < QSH; zl += 8) {
+                // this column's values along z, shared by the 4 rows' z-stencils:
+                // vz, wz at velocity-tile rows zb0 .. zb0+6, vx at rows zb0+1 .. zb0+7
+                const float *VXc = sv + 0 * PV_FLOATS + lx + 2, *VZc = sv + 1 * PV_FLOATS + lx + 2;
+                const float *WXc = sv + 2 * PV_FLOATS + lx + 2, *WZc = sv + 3 * PV_FLOATS + lx + 2;
+                float vzc[ROWS + 3], wzc[ROWS + 3], vxc[ROWS + 3];
+                uint8_t idc[ROWS + 1];
+#pragma unroll
+                for (int i = 0; i < ROWS + 3; ++i) {
+                    vzc[i] = VZc[(zb0 + i) * TMA_VW];
+                    wzc[i] = WZc[(zb0 + i) * TMA_VW];
+                    vxc[i] = VXc[(zb0 + 1 + i) * TMA_VW];
+                }
+#pragma unroll
+                for (int i = 0; i < ROWS + 1; ++i) idc[i] = si[(zb0 + i) * IW + lx + 2];
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int zl = zb0 + r;
                     const int z = z0 - 2 + zl;
                     const int pzo = zl + 2;                      // z in the profile slice
-                    const int vo = (zl + 2) * TMA_VW + lx + 2;      // in the velocity tile
-                    const int so = zl * TMA_VW + lx + 2;            // in the state tile
-                    const float *VXs = sv + 0 * PV_FLOATS + vo, *VZs = sv + 1 * PV_FLOATS + vo;
-                    const float *WXs = sv + 2 * PV_FLOATS + vo, *WZs = sv + 3 * PV_FLOATS + vo;
+                    const int vr = (zl + 2) * TMA_VW;            // row of the velocity tile
+                    const int so = zl * TMA_VW + lx + 2;         // in the state tile
                     const bool z_ok = IN || (z >= 0 && z <= NZ);
                     const bool cell_ok = x_ok && z_ok;
                     const bool g1 = IN || (cell_ok && x_g1 && z >= 2 && z <= NZ - 2);   // cu:60-62
@@ -662,17 +674,17 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const bool g3 = IN || (cell_ok && x_g3 && z >= 2 && z <= NZ - 1);   // cu:237-239
                     const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
                     const int o = (z + ZH) * P + xi;
-                    const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
-                    const float vdz = D4<EXACT>(VZs[0], VZs[-TMA_VW], VZs[TMA_VW], VZs[-2 * TMA_VW], m.qz);
-                    const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
-                    const float wdz = D4<EXACT>(WZs[0], WZs[-TMA_VW], WZs[TMA_VW], WZs[-2 * TMA_VW], m.qz);
-                    const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
-                    const float sdz = D4<EXACT>(VXs[TMA_VW], VXs[0], VXs[2 * TMA_VW], VXs[-TMA_VW], m.qz);
+                    const float vdx = D4<EXACT>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], m.qx);
+                    const float vdz = D4<EXACT>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], m.qz);
+                    const float wdx = D4<EXACT>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], m.qx);
+                    const float wdz = D4<EXACT>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], m.qz);
+                    const float sdx = D4<EXACT>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], m.qx);
+                    const float sdz = D4<EXACT>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], m.qz);
                     float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
                     float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
                     float sxz = ss[PS_SXZ * PS_FLOATS + so];
-                    const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * si[zl * IW + lx + 2]);
-                    const float mu_top = st[MT_W * si[(zl + 1) * IW + lx + 2] + MT_MU];   // rmu[top] (cu:218)
+                    const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * idc[r]);
+                    const float mu_top = st[MT_W * idc[r + 1] + MT_MU];   // rmu[top] (cu:218)
                     const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
                     const int zr = (!IN && z_ok) ? zrow(m, z) : -1;
                     float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
@@ -738,21 +750,21 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             }
             compute_sync();
 
-            // ---- receivers of this tile (vx, vz before the update; p of this step)
-            if (IM.nrec_q > 0) {
-                float *trace_row = IM.trace_row;
-                for (int q = tid; q < IM.nrec_q; q += PCT) {
-                    const int4 Rq = IM.rec[q];                   // (x, comp, slot, z)
-                    const int xl = Rq.x - x0, zl = Rq.w - z0;
-                    float v;
-                    if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
-                    else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
-                    trace_row[Rq.z] = v;
+            if (wid >= 2 * (QZ / ROWS)) {
+                // ---- receivers of this tile (vx, vz before the update; p of this step)
+                if (IM.nrec_q > 0) {
+                    float *trace_row = IM.trace_row;
+                    for (int q = tid - 32 * 2 * (QZ / ROWS); q < IM.nrec_q; q += PCT - 32 * 2 * (QZ / ROWS)) {
+                        const int4 Rq = IM.rec[q];               // (x, comp, slot, z)
+                        const int xl = Rq.x - x0, zl = Rq.w - z0;
+                        float v;
+                        if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
+                        else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
+                        trace_row[Rq.z] = v;
+                    }
                 }
-            }
-
-            // ---- velocity on the tile: column lx (< 60), rows ly, ly+8, ...
-            if (lx < QX) {
+            } else if (lx < QX) {
+                // ---- velocity on the tile: column lx (< 60), rows zb0 .. zb0+3
                 float *__restrict__ MXV = IM.mxv;
                 float *__restrict__ MZV = IM.mzv;
                 const int x = x0 + lx;
@@ -764,24 +776,37 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
                 const float bxh = PXs[PBH * PXW + pxo], axh = PXs[PAH * PXW + pxo];
                 const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo], Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
-#pragma unroll kPalVelUnroll
-                for (int zl = ly; zl < QZ; zl += 8) {
+                // this column's stress values along z: sxz at stress-tile rows
+                // zb0 .. zb0+6, szz and p at rows zb0+1 .. zb0+7
+                const float *SXXc = ss + PO_SXX * PS_FLOATS + lx + 4, *SZZc = ss + PO_SZZ * PS_FLOATS + lx + 4;
+                const float *SXZc = ss + PO_SXZ * PS_FLOATS + lx + 4, *PPc = ss + PO_P * PS_FLOATS + lx + 4;
+                float sxzc[ROWS + 3], szzc[ROWS + 3], ppc[ROWS + 3];
+                uint8_t idc[ROWS + 1];
+#pragma unroll
+                for (int i = 0; i < ROWS + 3; ++i) {
+                    sxzc[i] = SXZc[(zb0 + i) * TMA_VW];
+                    szzc[i] = SZZc[(zb0 + 1 + i) * TMA_VW];
+                    ppc[i] = PPc[(zb0 + 1 + i) * TMA_VW];
+                }
+#pragma unroll
+                for (int i = 0; i < ROWS + 1; ++i) idc[i] = si[(zb0 + 2 + i) * IW + lx + 4];
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int zl = zb0 + r;
                     const int t = z0 + zl;
                     if (!IN && (!x_in || t > NZ)) continue;
                     const int pzo = zl + 4;
-                    const int so = (zl + 2) * TMA_VW + lx + 4;      // (x, t) in the stress tile
-                    const float *SXX = ss + PO_SXX * PS_FLOATS + so, *SZZ = ss + PO_SZZ * PS_FLOATS + so;
-                    const float *SXZ = ss + PO_SXZ * PS_FLOATS + so, *PP = ss + PO_P * PS_FLOATS + so;
+                    const int sr = (zl + 2) * TMA_VW;            // row of the stress tile
                     const int vo = (zl + 4) * TMA_VW + lx + 4;
                     const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
                     const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
                     const int o = (t + ZH) * P + xi;
-                    const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
-                    const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
-                    const float d3x = D4<EXACT>(SXZ[0], SXZ[-TMA_VW], SXZ[TMA_VW], SXZ[-2 * TMA_VW], m.qz);
-                    const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
-                    const float d2z = D4<EXACT>(SZZ[TMA_VW], SZZ[0], SZZ[2 * TMA_VW], SZZ[-TMA_VW], m.qz);
-                    const float d3z = D4<EXACT>(PP[TMA_VW], PP[0], PP[2 * TMA_VW], PP[-TMA_VW], m.qz);
+                    const float d1x = D4<EXACT>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], m.qx);
+                    const float d2x = D4<EXACT>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], m.qx);
+                    const float d3x = D4<EXACT>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], m.qz);
+                    const float d1z = D4<EXACT>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], m.qx);
+                    const float d2z = D4<EXACT>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], m.qz);
+                    const float d3z = D4<EXACT>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], m.qz);
                     const bool gvx = IN || (x_vx && t >= 2 && t <= NZ - 1);   // cu:289-291
                     const bool gvz = IN || (x_vz && t >= 1 && t <= NZ - 2);   // cu:326-328
                     const int zr = IN ? -1 : zrow(m, t);
@@ -810,7 +835,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo], Kzh = KONE ? 1.0f : PZs[PKH * PZH + pzo];
                     float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
                     {   // vx, wx, material at (x, t) (cu:293-311)
-                        const float *mt = st + MT_W * si[(zl + 2) * IW + lx + 4];
+                        const float *mt = st + MT_W * idc[r];
                         const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
                         const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
                         const float rco = mt[MT_RCO];
@@ -821,7 +846,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         if (gvx) { wx1 = w1; vx1 = v1; }
                     }
                     {   // vz, wz, material at (x, t+1) (cu:330-353)
-                        const float *mt = st + MT_W * si[(zl + 3) * IW + lx + 4];
+                        const float *mt = st + MT_W * idc[r + 1];
                         const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
                         const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
                         const float rco = mt[MT_RCO];
