@@ -495,16 +495,58 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         int j = 0;
         for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
             const int b = j & 1;
-            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
-                if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
-                break;
-            }
-            unsigned char *buf = smp + b * BUF_BYTES;
+            // Resolve the item (a chain of dependent global loads) while buffer b
+            // is still being computed on, so the copies start the moment it frees.
             const int4 it = items[w];
             const ModelDev &m = MULTI ? models[it.x] : mp;
             const StreamShot &S = shots[it.y];
             const int x0 = it.z, z0 = it.w;
             const int P = m.P;
+            ItemMeta M;
+            const void *tm_v = nullptr, *tm_s = nullptr;
+            int cv = 0;
+            if (lane == 0) {
+                const int64_t n = *S.step + k + 1;
+                const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
+                M.FB = S.f[wr];
+                M.mxr = S.mx[rd];
+                M.mxw = S.mx[wr];
+                M.mzr = S.mz[rd];
+                M.mzw = S.mz[wr];
+                M.mxv = S.mxv;
+                M.mzv = S.mzv;
+                M.acc_w = S.acc + wr;
+                M.pacc = S.acc[rd];
+                M.src_off = (int)S.src_off;
+                M.src_where = S.src_where;
+                M.src_on = n <= S.src_n;
+                M.src_val = n <= S.src_n ? S.src_tab[n - 1] : 0.0f;
+                const bool rec_on = S.nrec > 0 && n <= S.trace_cap;
+                const int tile = (z0 / QZ) * m.ntx + x0 / QX;
+                const int qb = rec_on ? S.rec_start[tile] : 0, qe = rec_on ? S.rec_start[tile + 1] : 0;
+                M.rec = S.rec_sorted + qb;
+                M.nrec_q = qe - qb;
+                M.trace_row = rec_on ? S.trace + (n - 1) * S.nrec : nullptr;
+                M.x0 = x0;
+                M.z0 = z0;
+                // interior: no grid edge, C-PML strip or source within the tile and its halo
+                int sx = -1000000, sz = -1000000;
+                if (S.src_off >= 0) {
+                    sz = (int)(S.src_off / P) - ZH;
+                    sx = (int)(S.src_off - (int64_t)(sz + ZH) * P) - XH;
+                }
+                const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
+                M.interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
+                             zb <= m.NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
+                tm_v = S.tm_v;
+                tm_s = S.tm_s;
+                cv = rd * NSF;
+            }
+            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
+                if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
+                break;
+            }
+            unsigned char *buf = smp + b * BUF_BYTES;
             // ids, profile slices and the material table: cp.async, tracked by full[b]
             {
                 const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
@@ -536,50 +578,17 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             // every lane's cp.async tracking is on full[b] before lane 0's arrival can complete the phase
             __syncwarp();
             if (lane == 0) {
-                const int64_t n = *S.step + k + 1;
-                const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
-                ItemMeta &M = *reinterpret_cast<ItemMeta *>(buf + BUF_OFF_M);
-                M.FB = S.f[wr];
-                M.mxr = S.mx[rd];
-                M.mxw = S.mx[wr];
-                M.mzr = S.mz[rd];
-                M.mzw = S.mz[wr];
-                M.mxv = S.mxv;
-                M.mzv = S.mzv;
-                M.acc_w = S.acc + wr;
-                M.pacc = S.acc[rd];
-                M.src_off = (int)S.src_off;
-                M.src_where = S.src_where;
-                M.src_on = n <= S.src_n;
-                M.src_val = n <= S.src_n ? S.src_tab[n - 1] : 0.0f;
-                const bool rec_on = S.nrec > 0 && n <= S.trace_cap;
-                const int tile = (z0 / QZ) * m.ntx + x0 / QX;
-                const int qb = rec_on ? S.rec_start[tile] : 0, qe = rec_on ? S.rec_start[tile + 1] : 0;
-                M.rec = S.rec_sorted + qb;
-                M.nrec_q = qe - qb;
-                M.trace_row = rec_on ? S.trace + (n - 1) * S.nrec : nullptr;
-                M.x0 = x0;
-                M.z0 = z0;
-                // interior: no grid edge, C-PML strip or source within the tile and its halo
-                int sx = -1000000, sz = -1000000;
-                if (S.src_off >= 0) {
-                    sz = (int)(S.src_off / P) - ZH;
-                    sx = (int)(S.src_off - (int64_t)(sz + ZH) * P) - XH;
-                }
-                const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
-                M.interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
-                             zb <= m.NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
                 // the 4 velocity planes with a 4-cell halo and the 5 state planes with a 2-row halo
-                const int cv = rd * NSF;
                 float *sv = reinterpret_cast<float *>(buf);
                 float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
+                *reinterpret_cast<ItemMeta *>(buf + BUF_OFF_M) = M;
                 mbar_expect_tx(&full[b], PAL_TX_BYTES);
-                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, S.tm_v, x0, z0, cv + SF_VX + f, &full[b]);
-                tma_load_3d(ss + PS_G11 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
-                tma_load_3d(ss + PS_G22 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
-                tma_load_3d(ss + PS_XI1 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
-                tma_load_3d(ss + PS_XI2 * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
-                tma_load_3d(ss + PS_SXZ * PS_FLOATS, S.tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, tm_v, x0, z0, cv + SF_VX + f, &full[b]);
+                tma_load_3d(ss + PS_G11 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
+                tma_load_3d(ss + PS_G22 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
+                tma_load_3d(ss + PS_XI1 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
+                tma_load_3d(ss + PS_XI2 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
+                tma_load_3d(ss + PS_SXZ * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
             }
             __syncwarp();
         }
@@ -602,8 +611,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
         const int b = j & 1;
         unsigned char *buf = smp + b * BUF_BYTES;
-        // a bounded wait that gave up in any compute thread ends all of them together
-        if (!compute_sync_and(mbar_wait(&full[b], (uint32_t)((j >> 1) & 1)))) {
+        // No barrier here: warps run ahead into the item as soon as its data
+        // has landed.  A wait that gave up leaves the buffer's contents (item
+        // parameters included) untrusted: touch nothing, join the item's
+        // mid-point barrier, which then ends every compute thread together.
+        if (!mbar_wait(&full[b], (uint32_t)((j >> 1) & 1))) {
+            compute_sync_and(false);
             if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
             return;
         }
@@ -630,7 +643,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
 
         // Interior tiles (no grid edge, C-PML strip or source within the tile
         // and its halo) take a copy of the code with every guard constant-true.
-        auto compute = [&](auto interior_tag) {
+        auto compute = [&](auto interior_tag) -> bool {
             constexpr bool IN = decltype(interior_tag)::value;
             // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
             {
@@ -748,7 +761,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ss[PO_SXZ * PS_FLOATS + so] = sxz;
                 }
             }
-            compute_sync();
+            if (!compute_sync_and(true)) return false;   // false: a thread's wait for this item gave up
 
             if (wid >= 2 * (QZ / ROWS)) {
                 // ---- receivers of this tile (vx, vz before the update; p of this step)
@@ -863,9 +876,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     FB[SF_WZ * PL + o] = wz1;
                 }
             }
+            return true;
         };
-        if (IM.interior) compute(std::true_type{});
-        else compute(std::false_type{});
+        if (!(IM.interior ? compute(std::true_type{}) : compute(std::false_type{}))) {
+            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
+            return;
+        }
         // hand buffer b back to the producer
         fence_proxy_async();
         __syncwarp();
