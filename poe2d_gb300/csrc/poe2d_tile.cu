@@ -67,12 +67,6 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
@@ -445,6 +439,12 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar)
 {
     asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// add bytes to the current phase's transaction count without arriving
+__device__ __forceinline__ void mbar_expect_tx_only(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -547,6 +547,19 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 break;
             }
             unsigned char *buf = smp + b * BUF_BYTES;
+            if (lane == 0) {
+                // the big copies first: the 4 velocity planes with a 4-cell halo and
+                // the 5 state planes with a 2-row halo (bytes announced, no arrival yet)
+                float *sv = reinterpret_cast<float *>(buf);
+                float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
+                mbar_expect_tx_only(&full[b], PAL_TX_BYTES);
+                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, tm_v, x0, z0, cv + SF_VX + f, &full[b]);
+                tma_load_3d(ss + PS_G11 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
+                tma_load_3d(ss + PS_G22 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
+                tma_load_3d(ss + PS_XI1 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
+                tma_load_3d(ss + PS_XI2 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
+                tma_load_3d(ss + PS_SXZ * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+            }
             // ids, profile slices and the material table: cp.async, tracked by full[b]
             {
                 const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
@@ -575,20 +588,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 }
                 cp_async_mbar_arrive(&full[b]);
             }
-            // every lane's cp.async tracking is on full[b] before lane 0's arrival can complete the phase
+            // every lane's cp.async tracking is on full[b] before lane 0's arrival,
+            // the phase's only one, can complete it
             __syncwarp();
             if (lane == 0) {
-                // the 4 velocity planes with a 4-cell halo and the 5 state planes with a 2-row halo
-                float *sv = reinterpret_cast<float *>(buf);
-                float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
                 *reinterpret_cast<ItemMeta *>(buf + BUF_OFF_M) = M;
-                mbar_expect_tx(&full[b], PAL_TX_BYTES);
-                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, tm_v, x0, z0, cv + SF_VX + f, &full[b]);
-                tma_load_3d(ss + PS_G11 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
-                tma_load_3d(ss + PS_G22 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
-                tma_load_3d(ss + PS_XI1 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
-                tma_load_3d(ss + PS_XI2 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
-                tma_load_3d(ss + PS_SXZ * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+                mbar_arrive(&full[b]);
             }
             __syncwarp();
         }
