@@ -12,10 +12,20 @@ Inputs are synthetic (seeded), the reference ships no model files.
 
 value: Gcell-updates/s with the model resident in HBM (state reset + 20000
 steps per bench step, CUDA events around K steps).  e2e: the same through
-the C ABI from pinned host buffers: create context (coefficients H2D), run,
-read the traces back (D2H), destroy.  cpu_baseline / --impl reference: the
-CPU oracle (a C restatement of the reference loop, OpenMP over all host
-threads) on a bounded sample of steps of the same model.
+the C ABI from pinned host buffers: create context (coefficients in, palette
+built on the host, ids uploaded), run, read the traces back (D2H), destroy.
+cpu_baseline / --impl reference: the CPU oracle (a C restatement of the
+reference loop, OpenMP over all host threads) on a bounded sample of steps of
+the same model.
+
+batched (--batched M, default 64; 0 skips): the metric's "batched vs 1-shot"
+part.  (a) 64 shots of one 1001 x 1001 patchy model (30-cell C-PML, 10000
+steps, 256 receivers x 3 per shot) in one launch per step, against the same
+shots run one at a time; (b) M of the 256 uneven models (side U[256, 1536],
+steps 4 x side) in one batch, against back-to-back single-model runs.  Both
+check that the batched traces equal the single runs bit for bit.
+surrogate: gathers/s of the 4-member ensemble's forward passes at batch 256
+on the tensor cores, beside the batched solver's gathers/s on (b).
 
 Multi-GPU: shots are independent, so N ranks run N replicas (one shot each,
 sources shifted), with no collective on the data path ("scaling": "weak").
@@ -183,6 +193,36 @@ def leg_uneven(P, stream, fast, nmodels, seed=7):
             "cell_updates": work, "batched_gcells": work / t_b / 1e9, "back_to_back_gcells": work / t_1 / 1e9,
             "speedup_vs_back_to_back": t_1 / t_b, "batched_s": t_b, "back_to_back_s": t_1,
             "batched_launches": launches, "setup_s": setup, "first4_bitwise_equal_to_single_runs": same}
+
+
+def leg_surrogate(stream, solver_gathers_per_s, members=4, batch=256, reps=5):
+    """Inference throughput of the surrogate ensemble: every member's forward
+    pass over a batch of 256 inputs on the tensor cores (the weights do not
+    change the work; accuracy comes from poe2d_gb300.train_surrogate)."""
+    import torch
+    from poe2d_gb300.surrogate import CHANNELS, SAMPLES, Surrogate, forward_flops_per_sample
+    nets = [Surrogate(max_batch=batch, seed=k, stream=stream.cuda_stream) for k in range(members)]
+    g = torch.Generator().manual_seed(0)
+    maps = torch.rand((batch, 64, 64, 2), generator=g).to(torch.bfloat16).cuda()
+    sc = torch.rand((batch, 3), generator=g).cuda()
+    out = torch.empty((members, batch, SAMPLES, CHANNELS), device="cuda")
+
+    def run():
+        for k, net in enumerate(nets):
+            net.forward(maps, sc, out=out[k])
+    run()
+    run()
+    t = timed(stream, lambda: [run() for _ in range(reps)]) / reps
+    for net in nets:
+        net.close()
+    flops = forward_flops_per_sample() * batch * members
+    return {"gathers_per_s": batch / t, "members": members, "batch": batch, "s_per_batch": t,
+            "tensor_tflops": flops / t / 1e12, "solver_gathers_per_s": solver_gathers_per_s,
+            "speedup_vs_solver": (batch / t) / solver_gathers_per_s if solver_gathers_per_s else None,
+            "solver_sample": "the uneven batch above: models per second of the batched solver",
+            "heldout_rel_l2": None,
+            "accuracy": "not measured here: python -m poe2d_gb300.train_surrogate trains the ensemble on "
+                        "solver gathers and scores held-out models (solver fallback above 5 % spread)"}
 
 
 def alg_bytes_per_step(g, s_ctx_strips, per_cell=96):
@@ -460,14 +500,20 @@ def main():
             pg.all_reduce(te, op=pg.ReduceOp.MAX)
         el = float(te.item())
         e2e = {"value": cells * NSTEPS * e2e_steps * ws / el / 1e9, "unit": "Gcell-updates/s",
-               "h2d_bytes_per_step": int(coef.nbytes + px.nbytes + pz.nbytes + 12 * len(rec)),
+               # what the calls upload: material ids (1 B per cell, the palette
+               # is built on the host from the coefficient planes), the C-PML
+               # profiles, the receiver list and the source table
+               "h2d_bytes_per_step": int(ids.size + px.nbytes + pz.nbytes + 16 * len(rec) + 4 * NSTEPS),
                "d2h_bytes_per_step": int(htr.nbytes)}
     else:
         solver.close()
 
     batched = None
+    surrogate = None
     if args.batched > 0:
         batched = {"shots": leg_shots(P, stream, fast), "uneven": leg_uneven(P, stream, fast, args.batched)}
+        un = batched["uneven"]
+        surrogate = leg_surrogate(stream, args.batched / un["batched_s"])
 
     cb = None
     if rank == 0 and not args.no_cpu:
@@ -493,6 +539,7 @@ def main():
                          "palette_frac": alg_pal / step_s / 1e9 / hbm},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity, "batched": batched,
+            "surrogate": surrogate,
         }
         print(json.dumps(line), flush=True)
     if pg:

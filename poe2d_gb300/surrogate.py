@@ -17,6 +17,16 @@ from ._lib import PoeError
 
 MAP, MAP_CH, SCALARS, SAMPLES, CHANNELS = 64, 2, 3, 1024, 384
 
+# (GEMM rows per sample, reduction length, output channels) of every layer
+_LAYER_GEMMS = [(32 * 32, 18, 64), (16 * 16, 576, 128), (8 * 8, 1152, 128), (4 * 4, 1152, 256),
+                (1, 4099, 256), (1, 256, 2048), (32, 384, 128), (64, 384, 128), (128, 384, 128),
+                (256, 384, 64), (512, 192, 64), (1024, 192, 64), (1024, 192, 384)]
+
+
+def forward_flops_per_sample():
+    """Multiply-add FLOPs (2 per MAC) of one gather's forward pass."""
+    return sum(2 * m * k * n for m, k, n in _LAYER_GEMMS)
+
 
 class Surrogate:
     def __init__(self, max_batch=256, seed=0, stream=None):
