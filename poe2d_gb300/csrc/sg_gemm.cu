@@ -123,6 +123,9 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
     if (!ok) atomicExch(err, 1);
     const int row = m0 + warp * 32 + lane;
     const bool row_ok = row < M && nkb > 0;
+    // 16-byte vector stores where the row pitch keeps 16-column chunks aligned
+    const bool vec32 = (e.ldc % 4) == 0 && (((uintptr_t)(partial ? (void *)partial : (void *)e.out_f32)) & 15) == 0;
+    const bool vec16 = (e.ldc % 8) == 0 && (((uintptr_t)e.out_bf16) & 15) == 0;
 #pragma unroll 1
     for (int c = 0; c < BN / 16; ++c) {
         uint32_t v[16];
@@ -130,26 +133,68 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
         tmem_ld_wait();
         if (!row_ok || !ok) continue;
         const int nb = n0 + c * 16;
+        const bool full = nb + 16 <= N;
         if (partial) {   // split-K: raw partial sums
             float *p = partial + ((size_t)blockIdx.z * M + row) * e.ldc + nb;
+            if (full && vec32) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-                if (nb + j < N) p[j] = __uint_as_float(v[j]);
+                for (int q = 0; q < 4; ++q)
+                    reinterpret_cast<float4 *>(p)[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
+                                                                   __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (nb + j < N) p[j] = __uint_as_float(v[j]);
+            }
             continue;
         }
+        float x[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            const int n = nb + j;
-            if (n >= N) continue;
-            float x = e.alpha * __uint_as_float(v[j]);
-            if (e.bias) x += e.bias[n];
-            if (e.relu) x = fmaxf(x, 0.0f);
-            const size_t o = (size_t)row * e.ldc + n;
-            if (e.out_f32) {
-                if (e.accumulate) x += e.out_f32[o];
-                e.out_f32[o] = x;
+            float t = e.alpha * __uint_as_float(v[j]);
+            if (e.bias && nb + j < N) t += e.bias[nb + j];
+            if (e.relu) t = fmaxf(t, 0.0f);
+            x[j] = t;
+        }
+        const size_t o = (size_t)row * e.ldc + nb;
+        if (e.out_f32) {
+            float *p = e.out_f32 + o;
+            if (full && vec32) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float4 w = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+                    if (e.accumulate) {
+                        const float4 a = reinterpret_cast<const float4 *>(p)[q];
+                        w.x += a.x; w.y += a.y; w.z += a.z; w.w += a.w;
+                    }
+                    reinterpret_cast<float4 *>(p)[q] = w;
+                    x[4 * q] = w.x; x[4 * q + 1] = w.y; x[4 * q + 2] = w.z; x[4 * q + 3] = w.w;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (nb + j >= N) continue;
+                    if (e.accumulate) x[j] += p[j];
+                    p[j] = x[j];
+                }
             }
-            if (e.out_bf16) e.out_bf16[o] = __float2bfloat16_rn(x);
+        }
+        if (e.out_bf16) {
+            __nv_bfloat16 *p = e.out_bf16 + o;
+            if (full && vec16) {
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    uint4 w;
+                    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(x[8 * q + 2 * i], x[8 * q + 2 * i + 1]);
+                    reinterpret_cast<uint4 *>(p)[q] = w;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (nb + j < N) p[j] = __float2bfloat16_rn(x[j]);
+            }
         }
     }
     tc_fence_before();

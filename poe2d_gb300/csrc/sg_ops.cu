@@ -24,99 +24,152 @@ int grid_for(int64_t n, int block)
     return (int)(g < 1 ? 1 : g);
 }
 
+// Index arithmetic is 32-bit (every tensor here has fewer than 2^31 elements,
+// checked by the launchers) and the channel-vectorised kernels move 8 bf16
+// (16 bytes) per thread: channel counts that are multiples of 8 keep a group
+// of 8 consecutive columns inside one tap and one source pixel.
+
+__device__ __forceinline__ void add8(float (&acc)[8], const uint4 v)
+{
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 f = __bfloat1622float2(h[i]);
+        acc[2 * i] += f.x;
+        acc[2 * i + 1] += f.y;
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&acc)[8])
+{
+    uint4 v;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(acc[2 * i], acc[2 * i + 1]);
+    return v;
+}
+
 // conv 3x3, stride 2, pad 1: col[(b, oy, ox), (ky*3 + kx)*C + c], zero past 9C up to ld
 __global__ void k_im2col2d(const __nv_bfloat16 *x, int B, int H, int W, int C, __nv_bfloat16 *col, int ld)
 {
     const int Ho = H / 2, Wo = W / 2;
-    const int64_t total = (int64_t)B * Ho * Wo * ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(i % ld);
-        const int64_t r = i / ld;
+    const int total = B * Ho * Wo * ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int k = i % ld, r = i / ld;
         float v = 0.0f;
         if (k < 9 * C) {
             const int tap = k / C, c = k - tap * C;
             const int ky = tap / 3, kx = tap - ky * 3;
-            const int ox = (int)(r % Wo), oy = (int)((r / Wo) % Ho), b = (int)(r / ((int64_t)Wo * Ho));
+            const int ox = r % Wo, oy = (r / Wo) % Ho, b = r / (Wo * Ho);
             const int y = 2 * oy - 1 + ky, xx = 2 * ox - 1 + kx;
-            if (y >= 0 && y < H && xx >= 0 && xx < W) v = bf(x[(((int64_t)b * H + y) * W + xx) * C + c]);
+            if (y >= 0 && y < H && xx >= 0 && xx < W) v = bf(x[((b * H + y) * W + xx) * C + c]);
         }
         col[i] = tobf(v);
     }
 }
 
-// gradient of k_im2col2d: dx[b, y, x, c] = sum of the col entries that copied it
-__global__ void k_col2im2d(const __nv_bfloat16 *dcol, int ld, int B, int H, int W, int C, __nv_bfloat16 *dx)
+// the same for C % 8 == 0, 8 columns per thread
+__global__ void k_im2col2d_v8(const __nv_bfloat16 *x, int B, int H, int W, int C, __nv_bfloat16 *col, int ld)
 {
-    const int Ho = H / 2, Wo = W / 2;
-    const int64_t total = (int64_t)B * H * W * C;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const int xx = (int)((i / C) % W), y = (int)((i / ((int64_t)C * W)) % H);
-        const int b = (int)(i / ((int64_t)C * W * H));
-        float s = 0.0f;
+    const int Ho = H / 2, Wo = W / 2, U = ld / 8;
+    const int total = B * Ho * Wo * U;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int u = i % U, r = i / U;
+        const int k = 8 * u;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (k < 9 * C) {
+            const int tap = k / C, c = k - tap * C;
+            const int ky = tap / 3, kx = tap - ky * 3;
+            const int ox = r % Wo, oy = (r / Wo) % Ho, b = r / (Wo * Ho);
+            const int y = 2 * oy - 1 + ky, xx = 2 * ox - 1 + kx;
+            if (y >= 0 && y < H && xx >= 0 && xx < W)
+                v = *reinterpret_cast<const uint4 *>(x + ((b * H + y) * W + xx) * C + c);
+        }
+        *reinterpret_cast<uint4 *>(col + r * ld + k) = v;
+    }
+}
+
+// gradient of the im2col above: dx[b, y, x, c0..c0+7] = sum of the col entries that copied
+// it (C % 8 == 0)
+__global__ void k_col2im2d_v8(const __nv_bfloat16 *dcol, int ld, int B, int H, int W, int C, __nv_bfloat16 *dx)
+{
+    const int Ho = H / 2, Wo = W / 2, U = C / 8;
+    const int total = B * H * W * U;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = 8 * (i % U), p = i / U;
+        const int xx = p % W, y = (p / W) % H, b = p / (W * H);
+        float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         for (int ky = 0; ky < 3; ++ky) {
             const int ty = y + 1 - ky;
             if (ty < 0 || (ty & 1) || ty / 2 >= Ho) continue;
             for (int kx = 0; kx < 3; ++kx) {
                 const int tx = xx + 1 - kx;
                 if (tx < 0 || (tx & 1) || tx / 2 >= Wo) continue;
-                const int64_t r = ((int64_t)b * Ho + ty / 2) * Wo + tx / 2;
-                s += bf(dcol[r * ld + (ky * 3 + kx) * C + c]);
+                const int r = (b * Ho + ty / 2) * Wo + tx / 2;
+                add8(acc, *reinterpret_cast<const uint4 *>(dcol + r * ld + (ky * 3 + kx) * C + c));
             }
         }
-        dx[i] = tobf(s);
+        *reinterpret_cast<uint4 *>(dx + p * C + c) = pack8(acc);
     }
 }
 
 // conv1d k=3, pad 1, over x repeated `up` times in time:
-// col[(b, t), tap*C + c] = u[b, t + tap - 1, c], u[t] = x[t / up], To = T * up
-__global__ void k_im2col1d(const __nv_bfloat16 *x, int B, int T, int C, int up, __nv_bfloat16 *col, int ld)
+// col[(b, t), tap*C + c] = u[b, t + tap - 1, c], u[t] = x[t / up], To = T * up (C % 8 == 0)
+__global__ void k_im2col1d_v8(const __nv_bfloat16 *x, int B, int T, int C, int up, __nv_bfloat16 *col, int ld)
 {
-    const int To = T * up;
-    const int64_t total = (int64_t)B * To * ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(i % ld);
-        const int64_t r = i / ld;
-        float v = 0.0f;
+    const int To = T * up, U = ld / 8;
+    const int total = B * To * U;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int u = i % U, r = i / U;
+        const int k = 8 * u;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (k < 3 * C) {
             const int tap = k / C, c = k - tap * C;
-            const int t = (int)(r % To), b = (int)(r / To);
+            const int t = r % To, b = r / To;
             const int s = t + tap - 1;
-            if (s >= 0 && s < To) v = bf(x[((int64_t)b * T + s / up) * C + c]);
+            if (s >= 0 && s < To) v = *reinterpret_cast<const uint4 *>(x + (b * T + s / up) * C + c);
         }
-        col[i] = tobf(v);
+        *reinterpret_cast<uint4 *>(col + r * ld + k) = v;
     }
 }
 
-__global__ void k_col2im1d(const __nv_bfloat16 *dcol, int ld, int B, int T, int C, int up, __nv_bfloat16 *dx)
+__global__ void k_col2im1d_v8(const __nv_bfloat16 *dcol, int ld, int B, int T, int C, int up, __nv_bfloat16 *dx)
 {
-    const int To = T * up;
-    const int64_t total = (int64_t)B * T * C;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const int t = (int)((i / C) % T), b = (int)(i / ((int64_t)C * T));
-        float s = 0.0f;
+    const int To = T * up, U = C / 8;
+    const int total = B * T * U;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int c = 8 * (i % U), p = i / U;
+        const int t = p % T, b = p / T;
+        float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         for (int q = 0; q < up; ++q) {
             const int su = t * up + q;                    // a time of the upsampled input
             for (int tap = 0; tap < 3; ++tap) {
                 const int to = su - tap + 1;              // output time that read su through this tap
                 if (to < 0 || to >= To) continue;
-                s += bf(dcol[((int64_t)b * To + to) * ld + tap * C + c]);
+                add8(acc, *reinterpret_cast<const uint4 *>(dcol + (b * To + to) * ld + tap * C + c));
             }
         }
-        dx[i] = tobf(s);
+        *reinterpret_cast<uint4 *>(dx + p * C + c) = pack8(acc);
     }
 }
 
 // dz = dy * (y > 0); dy rows have pitch ldy, y and dz are dense rows x cols
-__global__ void k_relu_bwd(const __nv_bfloat16 *dy, int ldy, const __nv_bfloat16 *y, int64_t rows, int cols,
-                           __nv_bfloat16 *dz)
+// (cols and ldy multiples of 8: 8 elements per thread)
+__global__ void k_relu_bwd_v8(const __nv_bfloat16 *dy, int ldy, const __nv_bfloat16 *y, int rows, int cols,
+                              __nv_bfloat16 *dz)
 {
-    const int64_t total = rows * cols;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / cols;
-        const int c = (int)(i - r * cols);
-        dz[i] = bf(y[i]) > 0.0f ? dy[r * ldy + c] : tobf(0.0f);
+    const int U = cols / 8, total = rows * U;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int r = i / U, c = 8 * (i - r * U);
+        const uint4 g = *reinterpret_cast<const uint4 *>(dy + r * ldy + c);
+        const uint4 a = *reinterpret_cast<const uint4 *>(y + r * cols + c);
+        const __nv_bfloat16 *gh = reinterpret_cast<const __nv_bfloat16 *>(&g);
+        const __nv_bfloat16 *ah = reinterpret_cast<const __nv_bfloat16 *>(&a);
+        uint4 o;
+        __nv_bfloat16 *oh = reinterpret_cast<__nv_bfloat16 *>(&o);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) oh[j] = bf(ah[j]) > 0.0f ? gh[j] : tobf(0.0f);
+        *reinterpret_cast<uint4 *>(dz + r * cols + c) = o;
     }
 }
 
@@ -235,38 +288,48 @@ __global__ void k_concat(const __nv_bfloat16 *src, int ns, const float *extra, i
 }
 }  // namespace
 
+namespace {
+bool small(int64_t n) { return n < ((int64_t)1 << 31); }
+}  // namespace
+
 int im2col2d(const __nv_bfloat16 *x, int B, int H, int W, int C, __nv_bfloat16 *col, int ld, cudaStream_t st)
 {
     const int64_t n = (int64_t)B * (H / 2) * (W / 2) * ld;
-    k_im2col2d<<<grid_for(n, 256), 256, 0, st>>>(x, B, H, W, C, col, ld);
+    if (!small(n) || !small((int64_t)B * H * W * C)) return (int)cudaErrorInvalidValue;
+    if (C % 8 == 0 && ld % 8 == 0) k_im2col2d_v8<<<grid_for(n / 8, 256), 256, 0, st>>>(x, B, H, W, C, col, ld);
+    else k_im2col2d<<<grid_for(n, 256), 256, 0, st>>>(x, B, H, W, C, col, ld);
     return (int)cudaGetLastError();
 }
 
 int col2im2d(const __nv_bfloat16 *dcol, int ld, int B, int H, int W, int C, __nv_bfloat16 *dx, cudaStream_t st)
 {
     const int64_t n = (int64_t)B * H * W * C;
-    k_col2im2d<<<grid_for(n, 256), 256, 0, st>>>(dcol, ld, B, H, W, C, dx);
+    if (!small(n) || !small((int64_t)B * (H / 2) * (W / 2) * ld) || C % 8 || ld % 8) return (int)cudaErrorInvalidValue;
+    k_col2im2d_v8<<<grid_for(n / 8, 256), 256, 0, st>>>(dcol, ld, B, H, W, C, dx);
     return (int)cudaGetLastError();
 }
 
 int im2col1d(const __nv_bfloat16 *x, int B, int T, int C, int up, __nv_bfloat16 *col, int ld, cudaStream_t st)
 {
     const int64_t n = (int64_t)B * T * up * ld;
-    k_im2col1d<<<grid_for(n, 256), 256, 0, st>>>(x, B, T, C, up, col, ld);
+    if (!small(n) || C % 8 || ld % 8) return (int)cudaErrorInvalidValue;
+    k_im2col1d_v8<<<grid_for(n / 8, 256), 256, 0, st>>>(x, B, T, C, up, col, ld);
     return (int)cudaGetLastError();
 }
 
 int col2im1d(const __nv_bfloat16 *dcol, int ld, int B, int T, int C, int up, __nv_bfloat16 *dx, cudaStream_t st)
 {
     const int64_t n = (int64_t)B * T * C;
-    k_col2im1d<<<grid_for(n, 256), 256, 0, st>>>(dcol, ld, B, T, C, up, dx);
+    if (!small(n) || !small((int64_t)B * T * up * ld) || C % 8 || ld % 8) return (int)cudaErrorInvalidValue;
+    k_col2im1d_v8<<<grid_for(n / 8, 256), 256, 0, st>>>(dcol, ld, B, T, C, up, dx);
     return (int)cudaGetLastError();
 }
 
 int relu_bwd(const __nv_bfloat16 *dy, int ldy, const __nv_bfloat16 *y, int64_t rows, int cols, __nv_bfloat16 *dz,
              cudaStream_t st)
 {
-    k_relu_bwd<<<grid_for(rows * cols, 256), 256, 0, st>>>(dy, ldy, y, rows, cols, dz);
+    if (!small(rows * (int64_t)(cols > ldy ? cols : ldy)) || cols % 8 || ldy % 8) return (int)cudaErrorInvalidValue;
+    k_relu_bwd_v8<<<grid_for(rows * cols / 8, 256), 256, 0, st>>>(dy, ldy, y, (int)rows, cols, dz);
     return (int)cudaGetLastError();
 }
 
