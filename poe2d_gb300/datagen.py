@@ -62,15 +62,17 @@ def patchy_ids(shape, dx, fraction, r_mean, seed, spread=0.5):
     return ids
 
 
-def uneven_specs(seed, n, n_min=256, n_max=1536):
-    """n model specifications of the uneven batch (one row per model)."""
+def uneven_specs(seed, n, n_min=256, n_max=1536, gas_max=0.3, phi=(0.1, 0.3), f0=(150.0, 300.0)):
+    """n model specifications of the uneven batch (one row per model).
+    The ranges narrow the family (e.g. gas_max = 0: homogeneous
+    water-saturated models)."""
     rng = np.random.default_rng(seed)
     side = rng.integers(n_min, n_max + 1, n)
     out = []
     for i in range(n):
         out.append(dict(index=i, seed=int(seed) * 100003 + i, side=int(side[i]), steps=4 * int(side[i]),
-                        phi=float(rng.uniform(0.1, 0.3)), gas=float(rng.uniform(0.0, 0.3)),
-                        radius=float(rng.uniform(1.0, 10.0)), f0=float(rng.uniform(150.0, 300.0))))
+                        phi=float(rng.uniform(phi[0], phi[1])), gas=float(rng.uniform(0.0, gas_max)),
+                        radius=float(rng.uniform(1.0, 10.0)), f0=float(rng.uniform(f0[0], f0[1]))))
     return out
 
 

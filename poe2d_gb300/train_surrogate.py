@@ -133,6 +133,11 @@ def main(argv=None):
     ap.add_argument("--members", type=int, default=4)
     ap.add_argument("--threshold", type=float, default=0.05)
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--side-min", type=int, default=256)
+    ap.add_argument("--side-max", type=int, default=1536)
+    ap.add_argument("--gas-max", type=float, default=0.3, help="0: homogeneous (gas-free) models only")
+    ap.add_argument("--phi", type=float, nargs=2, default=(0.1, 0.3))
+    ap.add_argument("--f0", type=float, nargs=2, default=(150.0, 300.0))
     ap.add_argument("--out", default=None, help="write the summary JSON here")
     args = ap.parse_args(argv)
 
@@ -148,9 +153,11 @@ def main(argv=None):
     # 1. data: training realisations and held-out realisations from other seeds
     spec_tr = []
     for k in range(math.ceil(args.train / 256)):
-        spec_tr += D.uneven_specs(args.seed * 1000 + k, 256)
+        spec_tr += D.uneven_specs(args.seed * 1000 + k, 256, args.side_min, args.side_max, args.gas_max, args.phi,
+                                  args.f0)
     spec_tr = spec_tr[:args.train]
-    spec_ho = D.uneven_specs(args.seed * 1000 + 999, 256)[:args.heldout]
+    spec_ho = D.uneven_specs(args.seed * 1000 + 999, 256, args.side_min, args.side_max, args.gas_max, args.phi,
+                             args.f0)[:args.heldout]
     t0 = time.perf_counter()
     m_tr, s_tr, y_tr, ts_tr, c_tr = generate(spec_tr, stream)
     m_ho, s_ho, y_ho, ts_ho, c_ho = generate(spec_ho, stream)
@@ -212,6 +219,8 @@ def main(argv=None):
         _, _, _, t_fb, _ = generate(rej, stream)
     n = len(spec_ho)
     summary = {
+        "family": {"side": [args.side_min, args.side_max], "gas_max": args.gas_max, "phi": list(args.phi),
+                   "f0": list(args.f0)},
         "train_models": len(spec_tr), "heldout_models": n, "epochs": args.epochs, "batch": args.batch,
         "members": len(members), "params_per_member": members[0].nparam,
         "data_s": t_data, "solver_s_train": ts_tr, "solver_s_heldout": ts_ho,
