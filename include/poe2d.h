@@ -217,6 +217,23 @@ int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes);
 int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capacity);
 int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_t size);
 
+/* Tuning (no reference counterpart).  The palette kernel walks a list of
+ * (shot, tile) items, one CTA per SM; the order of that list decides which
+ * tiles run side by side (halo reuse in L2), and poe_run replays a captured
+ * CUDA graph of graph_steps steps.  Results do not depend on either. */
+enum {
+    POE_ORDER_ROWS = 0,       /* per shot, tile rows (the default) */
+    POE_ORDER_COLUMNS = 1,    /* per shot, tile columns */
+    POE_ORDER_TILE_MAJOR = 2  /* the same tile of every shot side by side */
+};
+int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
+
+/* Time every (order, graph_steps in {16, 64}) pair on this context for
+ * trial_steps steps, keep the fastest and report it; ms_out (may be NULL)
+ * receives the 6 timings, order-major.  Every shot must be at step 0; the
+ * shots are reset to step 0 afterwards. */
+int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out);
+
 /* Steps completed by a shot. */
 int poe_steps_done(poe_ctx *ctx, int32_t shot, int64_t *steps);
 

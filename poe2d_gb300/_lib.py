@@ -80,6 +80,8 @@ SYMBOLS = {
     "poe_checkpoint_size": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "poe_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "poe_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "poe_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _fp]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_reset_shot": (C.c_int, [C.c_void_p, C.c_int32]),
     "poe_check_finite": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, _fp]),

@@ -71,6 +71,8 @@ struct poe_ctx {
     float *mtab = nullptr;      // palette mode: material table
     int nmat = 0;
     int ntx = 1, ntz = 1;       // tiles across x and z
+    int order = 0;              // work-list order (POE_ORDER_*)
+    int graph_steps = kGraphSteps;   // steps per captured graph
     int tile_x = TILE_X, tile_z = TILE_Z;
     std::string err;
 };
@@ -193,12 +195,24 @@ int sync_shots(poe_ctx *ctx)
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
     }
-    // palette kernel work list: every tile of every shot, shot-major
+    // palette kernel work list: every tile of every shot, in the context's order
     ctx->items.clear();
-    if (ctx->ids)
-        for (int i = 0; i < ns; ++i)
+    if (ctx->ids) {
+        auto add = [&](int i, int tx, int tz) { ctx->items.push_back(make_int4(0, i, tx * PAL_TX, tz * PAL_TZ)); };
+        if (ctx->order == POE_ORDER_TILE_MAJOR) {        // the same tile of every shot side by side
             for (int tz = 0; tz < ctx->ntz; ++tz)
-                for (int tx = 0; tx < ctx->ntx; ++tx) ctx->items.push_back(make_int4(0, i, tx * PAL_TX, tz * PAL_TZ));
+                for (int tx = 0; tx < ctx->ntx; ++tx)
+                    for (int i = 0; i < ns; ++i) add(i, tx, tz);
+        } else if (ctx->order == POE_ORDER_COLUMNS) {    // per shot, tile columns
+            for (int i = 0; i < ns; ++i)
+                for (int tx = 0; tx < ctx->ntx; ++tx)
+                    for (int tz = 0; tz < ctx->ntz; ++tz) add(i, tx, tz);
+        } else {                                         // per shot, tile rows
+            for (int i = 0; i < ns; ++i)
+                for (int tz = 0; tz < ctx->ntz; ++tz)
+                    for (int tx = 0; tx < ctx->ntx; ++tx) add(i, tx, tz);
+        }
+    }
     const int ni = (int)ctx->items.size();
     if (ni > ctx->items_dev_cap) {
         cudaFree(ctx->items_dev);
@@ -288,9 +302,9 @@ int build_graph(poe_ctx *ctx)
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
-    for (int k = 0; k < kGraphSteps && rc == 0; ++k)
+    for (int k = 0; k < ctx->graph_steps && rc == 0; ++k)
         rc = step_launch(ctx, k);
-    if (rc == 0) rc = launch_advance(ctx->steps_dev, ns, kGraphSteps, ctx->stream);
+    if (rc == 0) rc = launch_advance(ctx->steps_dev, ns, ctx->graph_steps, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -303,7 +317,7 @@ int build_graph(poe_ctx *ctx)
         ctx->graph = nullptr;
         return fail(ctx, POE_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
-    ctx->graph_kernels = kGraphSteps * kernels_per_step(ctx) + 1;
+    ctx->graph_kernels = ctx->graph_steps * kernels_per_step(ctx) + 1;
     return POE_OK;
 }
 
@@ -650,9 +664,9 @@ int poe_run(poe_ctx *ctx, int64_t nsteps)
     }
     if ((rc = sync_shots(ctx)) != POE_OK) return rc;
     int64_t left = nsteps;
-    if (left >= kGraphSteps) {
+    if (left >= ctx->graph_steps) {
         if (!ctx->graph && (rc = build_graph(ctx)) != POE_OK) return rc;
-        for (; left >= kGraphSteps; left -= kGraphSteps) {
+        for (; left >= ctx->graph_steps; left -= ctx->graph_steps) {
             CK(cudaGraphLaunch(ctx->graph, ctx->stream));
             ctx->launches += ctx->graph_kernels;
         }
@@ -952,6 +966,61 @@ int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_
     s->steps = h.steps;
     ctx->shots_dirty = true;
     return sync_shots(ctx);
+}
+
+int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps)
+{
+    if (!ctx) return POE_EINVAL;
+    if (order < POE_ORDER_ROWS || order > POE_ORDER_TILE_MAJOR || graph_steps < 1 || graph_steps > 4096)
+        return fail(ctx, POE_EINVAL, "tuning: order or graph_steps out of range");
+    if (order != ctx->order) ctx->shots_dirty = true;   // rebuilds the work list (and the graph)
+    if (graph_steps != ctx->graph_steps) drop_graph(ctx);
+    ctx->order = order;
+    ctx->graph_steps = graph_steps;
+    return POE_OK;
+}
+
+int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out)
+{
+    if (!ctx || trial_steps < 1) return POE_EINVAL;
+    if (ctx->shots.empty()) return fail(ctx, POE_ESTATE, "autotune: no shots");
+    for (const ShotHost &s : ctx->shots)
+        if (s.steps != 0) return fail(ctx, POE_ESTATE, "autotune: every shot must be at step 0 (it is reset after)");
+    CK(cudaSetDevice(ctx->device));
+    static const int32_t kSteps[2] = {16, 64};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int best = -1, rc = POE_OK;
+    float best_ms = 0.0f;
+    for (int c = 0; c < 3 * 2 && rc == POE_OK; ++c) {
+        const int order = c / 2, gs = kSteps[c % 2];
+        if ((rc = poe_tune(ctx, order, gs)) != POE_OK) break;
+        if ((rc = poe_run(ctx, gs)) != POE_OK) break;        // capture the graph, first touch
+        cudaEventRecord(e0, ctx->stream);
+        if ((rc = poe_run(ctx, trial_steps)) != POE_OK) break;
+        cudaEventRecord(e1, ctx->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = fail(ctx, POE_ECUDA, "autotune: event");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms_out) ms_out[c] = ms;
+        if (best < 0 || ms < best_ms) {
+            best = c;
+            best_ms = ms;
+        }
+        if ((rc = device_status(ctx)) != POE_OK) break;
+        for (int i = 0; i < (int)ctx->shots.size() && rc == POE_OK; ++i) rc = poe_reset_shot(ctx, i);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != POE_OK) return rc;
+    rc = poe_tune(ctx, best / 2, kSteps[best % 2]);
+    if (order_out) *order_out = best / 2;
+    if (graph_steps_out) *graph_steps_out = kSteps[best % 2];
+    return rc;
 }
 
 int poe_check_finite(poe_ctx *ctx, int32_t shot, float threshold, float *max_abs_out)

@@ -1,0 +1,64 @@
+"""The autotuner times the work-list orders and graph lengths on the context
+itself, keeps the fastest, and leaves the shots at step 0; whatever it picks,
+the results equal the default configuration's bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(poe):
+    from poe2d_gb300.patchy import random_patches
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = poe.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    gas = poe.biot_material(rho_f=100.0, k_f=0.02e9, eta=1e-5, **frame)
+    NX, NZ = 300, 200
+    ids = random_patches((NZ + 1, NX + 1), 0.5, fraction=0.15, r_min=1.0, r_max=4.0, seed=21)
+    coef, vp = poe.coeffs_biot([water, gas], ids)
+    g = poe.grid(NX, NZ, 0.5, 5e-5)
+    px, pz = poe.pml_profiles(g, 15, 200.0, vp)
+    rec = [(x, 18, c) for c in (0, 1, 2) for x in range(20, 280, 17)]
+    srcs = [poe.source(100 + 50 * k, 18, poe.SRC_RICKER_FZ, 200.0, 1e3, 0.0) for k in range(3)]
+    return g, coef, px, pz, rec, srcs
+
+
+def _run(poe, m, tune):
+    g, coef, px, pz, rec, srcs = m
+    with poe.Solver(g, coef, px, pz, fast=True) as s:
+        for src in srcs:
+            s.add_shot(src, rec)
+        picked = None
+        if tune == "auto":
+            picked = s.autotune(32)
+            assert all(s.steps(k) == 0 for k in range(len(srcs)))
+        elif tune is not None:
+            s.tune(*tune)
+        s.run(150)
+        return [s.traces(k) for k in range(len(srcs))] + [s.field("vz", 2)], picked
+
+
+def test_autotune_keeps_results_and_reports_timings(poe):
+    m = _model(poe)
+    ref, _ = _run(poe, m, None)
+    got, (order, gsteps, ms) = _run(poe, m, "auto")
+    assert order in (0, 1, 2) and gsteps in (16, 64)
+    assert np.all(ms > 0) and ms.argmin() == 2 * order + (1 if gsteps == 64 else 0)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    for tune in ((1, 16), (2, 64)):
+        other, _ = _run(poe, m, tune)
+        for a, b in zip(ref, other):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_tuning_arguments_are_checked(poe):
+    g, coef, px, pz, rec, srcs = _model(poe)
+    with poe.Solver(g, coef, px, pz) as s:
+        s.add_shot(srcs[0], rec)
+        with pytest.raises(poe.PoeError):
+            s.tune(3, 64)
+        with pytest.raises(poe.PoeError):
+            s.tune(0, 0)
+        s.run(5)
+        with pytest.raises(poe.PoeError):
+            s.autotune(8)                     # shots not at step 0
