@@ -32,25 +32,30 @@ namespace sg {
 using namespace sm103;
 
 namespace {
-constexpr int BM = 128, BK = 64, STAGES = 4, NT = 128;
+constexpr int BM = 128, BK = 64, NT = 128;
 
-template <int BN>
+// ST pipeline stages: 4 for long reductions; 2 when a CTA sees at most 4
+// k-blocks, which keeps shared memory small enough for 3-4 CTAs per SM so
+// one CTA's epilogue overlaps another's loads and MMAs
+template <int BN, int ST>
 struct GemmSmem {
+    static constexpr int STAGES = ST;
     static constexpr int A_BYTES = BM * BK * 2;             // 16 KB
     static constexpr int B_BYTES = BN * BK * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
     static constexpr int BAR_OFF = STAGES * STAGE;
-    static constexpr int TOTAL = BAR_OFF + (2 * STAGES + 1) * 8 + 8 + 1024;   // + alignment slack
+    static constexpr int BIAS_OFF = BAR_OFF + (2 * STAGES + 1) * 8 + 8;
+    static constexpr int TOTAL = BIAS_OFF + BN * 4 + 1024;   // + alignment slack
     static constexpr uint32_t TX = (uint32_t)STAGE;
     static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
 };
 
-template <int BN>
+template <int BN, int STAGES>
 __global__ void __launch_bounds__(NT, 1)
 k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int M, int N, int K,
        int kblocks_per_split, Epilogue e, float *partial, int *err)
 {
-    using L = GemmSmem<BN>;
+    using L = GemmSmem<BN, STAGES>;
     extern __shared__ unsigned char smraw[];
     unsigned char *sm = (unsigned char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + L::BAR_OFF);
@@ -74,6 +79,9 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
         mbar_fence_init();
     }
     if (warp == 2) tmem_alloc(tslot, L::TMEM_COLS);
+    // the tile's bias once, for the epilogue (zero past N or without a bias)
+    float *sbias = reinterpret_cast<float *>(sm + L::BIAS_OFF);
+    for (int i = tid; i < BN; i += NT) sbias[i] = (e.bias && n0 + i < N) ? e.bias[n0 + i] : 0.0f;
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -127,73 +135,80 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
     const bool vec32 = (e.ldc % 4) == 0 && (((uintptr_t)(partial ? (void *)partial : (void *)e.out_f32)) & 15) == 0;
     const bool vec16 = (e.ldc % 8) == 0 && (((uintptr_t)e.out_bf16) & 15) == 0;
 #pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-        uint32_t v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+    for (int c2 = 0; c2 < BN / 32; ++c2) {
+        // two 16-column TMEM loads in flight per wait
+        uint32_t vv[2][16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c2 * 32), vv[0]);
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c2 * 32 + 16), vv[1]);
         tmem_ld_wait();
         if (!row_ok || !ok) continue;
-        const int nb = n0 + c * 16;
-        const bool full = nb + 16 <= N;
-        if (partial) {   // split-K: raw partial sums
-            float *p = partial + ((size_t)blockIdx.z * M + row) * e.ldc + nb;
-            if (full && vec32) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    reinterpret_cast<float4 *>(p)[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
-                                                                   __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
-            } else {
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    if (nb + j < N) p[j] = __uint_as_float(v[j]);
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t (&v)[16] = vv[h];
+            const int c = 2 * c2 + h;
+            const int nb = n0 + c * 16;
+            const bool full = nb + 16 <= N;
+            if (partial) {   // split-K: raw partial sums
+                float *p = partial + ((size_t)blockIdx.z * M + row) * e.ldc + nb;
+                if (full && vec32) {
+    #pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        reinterpret_cast<float4 *>(p)[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
+                                                                       __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
+                } else {
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (nb + j < N) p[j] = __uint_as_float(v[j]);
+                }
+                continue;
             }
-            continue;
-        }
-        float x[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            float t = e.alpha * __uint_as_float(v[j]);
-            if (e.bias && nb + j < N) t += e.bias[nb + j];
-            if (e.relu) t = fmaxf(t, 0.0f);
-            x[j] = t;
-        }
-        const size_t o = (size_t)row * e.ldc + nb;
-        if (e.out_f32) {
-            float *p = e.out_f32 + o;
-            if (full && vec32) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    float4 w = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
-                    if (e.accumulate) {
-                        const float4 a = reinterpret_cast<const float4 *>(p)[q];
-                        w.x += a.x; w.y += a.y; w.z += a.z; w.w += a.w;
+            float x[16];
+    #pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float t = e.alpha * __uint_as_float(v[j]);
+                t += sbias[c * 16 + j];
+                if (e.relu) t = fmaxf(t, 0.0f);
+                x[j] = t;
+            }
+            const size_t o = (size_t)row * e.ldc + nb;
+            if (e.out_f32) {
+                float *p = e.out_f32 + o;
+                if (full && vec32) {
+    #pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        float4 w = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+                        if (e.accumulate) {
+                            const float4 a = reinterpret_cast<const float4 *>(p)[q];
+                            w.x += a.x; w.y += a.y; w.z += a.z; w.w += a.w;
+                        }
+                        reinterpret_cast<float4 *>(p)[q] = w;
+                        x[4 * q] = w.x; x[4 * q + 1] = w.y; x[4 * q + 2] = w.z; x[4 * q + 3] = w.w;
                     }
-                    reinterpret_cast<float4 *>(p)[q] = w;
-                    x[4 * q] = w.x; x[4 * q + 1] = w.y; x[4 * q + 2] = w.z; x[4 * q + 3] = w.w;
-                }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    if (nb + j >= N) continue;
-                    if (e.accumulate) x[j] += p[j];
-                    p[j] = x[j];
+                } else {
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        if (nb + j >= N) continue;
+                        if (e.accumulate) x[j] += p[j];
+                        p[j] = x[j];
+                    }
                 }
             }
-        }
-        if (e.out_bf16) {
-            __nv_bfloat16 *p = e.out_bf16 + o;
-            if (full && vec16) {
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    uint4 w;
-                    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(x[8 * q + 2 * i], x[8 * q + 2 * i + 1]);
-                    reinterpret_cast<uint4 *>(p)[q] = w;
+            if (e.out_bf16) {
+                __nv_bfloat16 *p = e.out_bf16 + o;
+                if (full && vec16) {
+    #pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        uint4 w;
+                        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+    #pragma unroll
+                        for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(x[8 * q + 2 * i], x[8 * q + 2 * i + 1]);
+                        reinterpret_cast<uint4 *>(p)[q] = w;
+                    }
+                } else {
+    #pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (nb + j < N) p[j] = __float2bfloat16_rn(x[j]);
                 }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    if (nb + j < N) p[j] = __float2bfloat16_rn(x[j]);
             }
         }
     }
@@ -267,17 +282,18 @@ int sm_count()
     return sms;
 }
 
-template <int BN>
+template <int BN, int ST>
 int launch(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, int splits, int kper, const Epilogue &e,
            float *ws, int *err, cudaStream_t st)
 {
+    using L = GemmSmem<BN, ST>;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmSmem<BN>::TOTAL);
+        cudaFuncSetAttribute(k_gemm<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL);
         attr = true;
     }
     const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
-    k_gemm<BN><<<grid, NT, GemmSmem<BN>::TOTAL, st>>>(ta, tb, M, N, K, kper, e, splits > 1 ? ws : nullptr, err);
+    k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, M, N, K, kper, e, splits > 1 ? ws : nullptr, err);
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -305,8 +321,11 @@ int gemm(const Gemm &g, const Epilogue &e, float *ws, int64_t ws_floats, int *er
     }
     const int kper = (nkb + splits - 1) / splits;
     splits = (nkb + kper - 1) / kper;
-    int rc = BN == 128 ? launch<128>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
-                       : launch<64>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st);
+    const bool short_k = kper <= 4;
+    int rc = BN == 128 ? (short_k ? launch<128, 2>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
+                                  : launch<128, 4>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st))
+                       : (short_k ? launch<64, 2>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
+                                  : launch<64, 4>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st));
     if (rc || splits == 1) return rc;
     const int64_t total = (int64_t)g.M * g.N;
     int blocks = (int)((total + 255) / 256);

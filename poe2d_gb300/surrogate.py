@@ -96,3 +96,45 @@ class Surrogate:
         n = C.c_int64(0)
         self._check(L.lib().poe_sg_launches(self.h, C.byref(n)))
         return n.value
+
+
+def _bench(argv=None):
+    """python -m poe2d_gb300.surrogate [--batch 256] [--members 4] [--reps 5]:
+    inference throughput of an ensemble (weights do not change the work)."""
+    import argparse
+    import json
+
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--members", type=int, default=4)
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args(argv)
+    st = torch.cuda.Stream()
+    torch.cuda.set_stream(st)
+    nets = [Surrogate(max_batch=a.batch, seed=k, stream=st.cuda_stream) for k in range(a.members)]
+    g = torch.Generator().manual_seed(0)
+    maps = torch.rand((a.batch, MAP, MAP, MAP_CH), generator=g).to(torch.bfloat16).cuda()
+    sc = torch.rand((a.batch, SCALARS), generator=g).cuda()
+    out = torch.empty((a.members, a.batch, SAMPLES, CHANNELS), device="cuda")
+
+    def run():
+        for k, net in enumerate(nets):
+            net.forward(maps, sc, out=out[k])
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(a.reps):
+        run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / a.reps
+    print(json.dumps({"gathers_per_s": a.batch / t, "members": a.members, "batch": a.batch,
+                      "tensor_tflops": forward_flops_per_sample() * a.batch * a.members / t / 1e12}))
+    for net in nets:
+        net.close()
+
+
+if __name__ == "__main__":
+    _bench()
