@@ -542,6 +542,15 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 tm_s = S.tm_s;
                 cv = rd * NSF;
             }
+            // batch items: this lane's words of the model descriptor, read now
+            constexpr int MDW = (int)(sizeof(ModelDev) / 4);
+            static_assert(MDW <= 64, "two descriptor words per producer lane");
+            uint32_t md0 = 0, md1 = 0;
+            if (MULTI) {
+                const uint32_t *msrc = reinterpret_cast<const uint32_t *>(&m);
+                if (lane < MDW) md0 = msrc[lane];
+                if (lane + 32 < MDW) md1 = msrc[lane + 32];
+            }
             if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
                 if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
                 break;
@@ -582,9 +591,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     float *t = reinterpret_cast<float *>(buf + BUF_OFF_T);
                     for (int i = lane; i < m.nmat * (MT_W / 4); i += 32) cp_async16(t + 4 * i, m.mtab + 4 * i);
                     // the model descriptor itself, for the compute warps
-                    const uint32_t *msrc = reinterpret_cast<const uint32_t *>(&m);
                     uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
-                    for (int i = lane; i < (int)(sizeof(ModelDev) / 4); i += 32) mdst[i] = msrc[i];
+                    if (lane < MDW) mdst[lane] = md0;
+                    if (lane + 32 < MDW) mdst[lane + 32] = md1;
                 }
                 cp_async_mbar_arrive(&full[b]);
             }
@@ -626,6 +635,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             return;
         }
         const ModelDev &m = MULTI ? *reinterpret_cast<const ModelDev *>(buf + BUF_OFF_MD) : mp;
+        // the stencil divisors in registers: the model descriptor of a batch item
+        // sits in shared memory, where the loops' own stores would force re-reads
+        const Div24 qx = m.qx, qz = m.qz;
         const ItemMeta &IM = *reinterpret_cast<const ItemMeta *>(buf + BUF_OFF_M);
         const float *st = reinterpret_cast<const float *>(MULTI ? buf + BUF_OFF_T : smp + BUF_OFF_T);
         const float *PXs = reinterpret_cast<const float *>(buf + BUF_OFF_PX);
@@ -692,12 +704,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const bool g3 = IN || (cell_ok && x_g3 && z >= 2 && z <= NZ - 1);   // cu:237-239
                     const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
                     const int o = (z + ZH) * P + xi;
-                    const float vdx = D4<EXACT>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], m.qx);
-                    const float vdz = D4<EXACT>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], m.qz);
-                    const float wdx = D4<EXACT>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], m.qx);
-                    const float wdz = D4<EXACT>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], m.qz);
-                    const float sdx = D4<EXACT>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], m.qx);
-                    const float sdz = D4<EXACT>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], m.qz);
+                    const float vdx = D4<EXACT>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], qx);
+                    const float vdz = D4<EXACT>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], qz);
+                    const float wdx = D4<EXACT>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], qx);
+                    const float wdz = D4<EXACT>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], qz);
+                    const float sdx = D4<EXACT>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], qx);
+                    const float sdz = D4<EXACT>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], qz);
                     float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
                     float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
                     float sxz = ss[PS_SXZ * PS_FLOATS + so];
@@ -819,12 +831,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
                     const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
                     const int o = (t + ZH) * P + xi;
-                    const float d1x = D4<EXACT>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], m.qx);
-                    const float d2x = D4<EXACT>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], m.qx);
-                    const float d3x = D4<EXACT>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], m.qz);
-                    const float d1z = D4<EXACT>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], m.qx);
-                    const float d2z = D4<EXACT>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], m.qz);
-                    const float d3z = D4<EXACT>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], m.qz);
+                    const float d1x = D4<EXACT>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], qx);
+                    const float d2x = D4<EXACT>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], qx);
+                    const float d3x = D4<EXACT>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], qz);
+                    const float d1z = D4<EXACT>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], qx);
+                    const float d2z = D4<EXACT>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], qz);
+                    const float d3z = D4<EXACT>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], qz);
                     const bool gvx = IN || (x_vx && t >= 2 && t <= NZ - 1);   // cu:289-291
                     const bool gvz = IN || (x_vz && t >= 1 && t <= NZ - 2);   // cu:326-328
                     const int zr = IN ? -1 : zrow(m, t);
