@@ -542,6 +542,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 tm_s = S.tm_s;
                 cv = rd * NSF;
             }
+            // what the fills below need from the model, read now: past the wait
+            // (a compiler barrier) a batch item's descriptor would be re-read from
+            // global memory on the copies' critical path
+            const uint8_t *m_ids = m.ids;
+            const float *m_px = m.px, *m_pz = m.pz, *m_mtab = m.mtab;
+            const int m_R = m.R, m_nmat = m.nmat;
             // batch items: this lane's words of the model descriptor, read now
             constexpr int MDW = (int)(sizeof(ModelDev) / 4);
             static_assert(MDW <= 64, "two descriptor words per producer lane");
@@ -571,7 +577,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             }
             // ids, profile slices and the material table: cp.async, tracked by full[b]
             {
-                const unsigned char *src = m.ids + (int64_t)(z0 + 2) * P + x0;
+                const unsigned char *src = m_ids + (int64_t)(z0 + 2) * P + x0;
                 unsigned char *dst = buf + BUF_OFF_I;
                 for (int i = lane; i < IH * (IW / 4); i += 32) {
                     const int r = i / (IW / 4), c = i - r * (IW / 4);
@@ -581,15 +587,15 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 float *pz = reinterpret_cast<float *>(buf + BUF_OFF_PZ);
                 for (int i = lane; i < 6 * (PXW / 4); i += 32) {
                     const int r = i / (PXW / 4), c = i - r * (PXW / 4);
-                    cp_async16(px + r * PXW + 4 * c, m.px + (int64_t)r * P + x0 + 4 * c);
+                    cp_async16(px + r * PXW + 4 * c, m_px + (int64_t)r * P + x0 + 4 * c);
                 }
                 for (int i = lane; i < 6 * (PZH / 4); i += 32) {
                     const int r = i / (PZH / 4), c = i - r * (PZH / 4);
-                    cp_async16(pz + r * PZH + 4 * c, m.pz + (int64_t)r * m.R + z0 + 4 * c);
+                    cp_async16(pz + r * PZH + 4 * c, m_pz + (int64_t)r * m_R + z0 + 4 * c);
                 }
                 if (MULTI) {
                     float *t = reinterpret_cast<float *>(buf + BUF_OFF_T);
-                    for (int i = lane; i < m.nmat * (MT_W / 4); i += 32) cp_async16(t + 4 * i, m.mtab + 4 * i);
+                    for (int i = lane; i < m_nmat * (MT_W / 4); i += 32) cp_async16(t + 4 * i, m_mtab + 4 * i);
                     // the model descriptor itself, for the compute warps
                     uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
                     if (lane < MDW) mdst[lane] = md0;
