@@ -68,6 +68,7 @@ struct poe_ctx {
     float *derived = nullptr;   // 3 planes: sigma_xx, sigma_zz, p on demand
     int *err_dev = nullptr;     // set by a kernel whose bounded wait gave up
     uint8_t *ids = nullptr;     // palette mode: material id plane
+    CUtensorMap *tm_model = nullptr;   // palette mode: TMA descriptors of ids, px, pz (device)
     float *mtab = nullptr;      // palette mode: material table
     int nmat = 0;
     int ntx = 1, ntz = 1;       // tiles across x and z
@@ -353,6 +354,21 @@ EncodeTiledFn encode_fn()
     return fn;
 }
 
+// TMA descriptor of a 2-D array (d0 elements per row, d1 rows, rows stride
+// bytes apart) with a (box_w x box_h) box
+bool encode_2d(CUtensorMap *out, CUtensorMapDataType type, void *base, int64_t d0, int64_t d1, int64_t stride,
+               int box_w, int box_h)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)d0, (cuuint64_t)d1};
+    cuuint64_t strides[1] = {(cuuint64_t)stride};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    cuuint32_t es[2] = {1, 1};
+    return fn(out, type, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // TMA descriptor of a stack of float planes (pitch P, R rows, nplanes) with a
 // (box_w x box_h x 1) box
 bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes, int box_w, int box_h)
@@ -531,6 +547,17 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("upload: ") + cudaGetErrorString(e));
     }
+    if (rc == POE_OK && ctx->ids) {
+        // the palette kernel's producer fetches each tile's ids and profile
+        // slices with TMA (rows of P bytes / P floats / R floats)
+        CUtensorMap tm[3];
+        bool ok = encode_2d(&tm[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, ctx->ids, m.P, m.R, m.P, PAL_IDS_W, PAL_IDS_H) &&
+                  encode_2d(&tm[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->px, m.P, 6, (int64_t)m.P * 4, TMA_VW, 6) &&
+                  encode_2d(&tm[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->pz, m.R, 6, (int64_t)m.R * 4, TMA_VH, 6);
+        cudaError_t e = ok ? cudaMalloc(&ctx->tm_model, sizeof(tm)) : cudaErrorInvalidValue;
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->tm_model, tm, sizeof(tm), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("TMA descriptors: ") + cudaGetErrorString(e));
+    }
     if (rc != POE_OK) {
         poe_destroy(ctx);
         return rc;
@@ -542,6 +569,9 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     m.ids = ctx->ids;
     m.mtab = ctx->mtab;
     m.nmat = ctx->nmat;
+    m.tm_ids = ctx->tm_model ? (const void *)&ctx->tm_model[0] : nullptr;
+    m.tm_px = ctx->tm_model ? (const void *)&ctx->tm_model[1] : nullptr;
+    m.tm_pz = ctx->tm_model ? (const void *)&ctx->tm_model[2] : nullptr;
     // tile geometry of the kernel this model runs on (receiver lists are per tile)
     ctx->tile_x = ctx->ids ? PAL_TX : TILE_X;
     ctx->tile_z = ctx->ids ? PAL_TZ : TILE_Z;
@@ -1069,6 +1099,7 @@ void poe_destroy(poe_ctx *ctx)
     cudaFree(ctx->err_dev);
     cudaFree(ctx->ids);
     cudaFree(ctx->mtab);
+    cudaFree(ctx->tm_model);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -53,6 +53,9 @@ struct ModelDev {
     const float *mtab;       // nmat rows of MT_W floats
     int nmat;
     int ntx;                 // tiles across x of the kernel this model runs on (receiver lists)
+    // palette mode: TMA descriptors (device memory) of the id plane and of the
+    // 6 x-profile and 6 z-profile rows, boxed for the palette kernel's tiles
+    const void *tm_ids, *tm_px, *tm_pz;
 };
 
 // material-table row: coefficients and the quantities the reference derives
@@ -122,6 +125,9 @@ int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, vo
 // 68 x 36 (stress state) floats
 constexpr int PAL_TX = 60, PAL_TZ = 32;
 constexpr int TMA_VW = PAL_TX + 8, TMA_VH = PAL_TZ + 8, TMA_SH = PAL_TZ + 4;
+// material-id box: rows z0-2 .. z0+34, 80 bytes from x0+XH-4 rounded down to
+// 16 bytes (a TMA box starts on a 16-byte column), covering x0-4 .. x0+63
+constexpr int PAL_IDS_W = 80, PAL_IDS_H = PAL_TZ + 5;
 int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream);
 // allocation-free read-out of one derived field (sigma_xx 0, sigma_zz 1, p 2)
 // through the library's static scratch plane; returns a cudaError_t

@@ -88,6 +88,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
     return false;
 }
 
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0, int c1, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// bytes (a multiple of 16, both addresses 16-byte aligned) global -> shared
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0, int c1, int c2, uint64_t *bar)
 {
     asm volatile(
@@ -383,7 +399,7 @@ constexpr int PCT = 576;                           // compute threads: 18 warps
 constexpr int ROWS = 4;                            // consecutive rows per compute thread
 constexpr int PNT = PCT + 32;                      // + the producer warp
 constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
-constexpr int IW = TMA_VW, IH = QZ + 5;            // ids: cols x0-4 .. x0+63, rows z0-2 .. z0+34
+constexpr int IW = PAL_IDS_W, IH = PAL_IDS_H;      // ids: rows z0-2 .. z0+34; column x0-4 at (x0 & 15)
 constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
 constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
 constexpr int PS_FLOATS = (PS_BOX + 31) / 32 * 32; // slot stride: 128-B aligned TMA destinations
@@ -391,19 +407,21 @@ constexpr int PXW = TMA_VW, PZH = TMA_VH;          // profile slices: x0-4 .. x0
 constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
 constexpr int BUF_OFF_I = BUF_OFF_S + 5 * PS_FLOATS * 4;
 constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
-constexpr int BUF_OFF_PZ = BUF_OFF_PX + 6 * PXW * 4;
-constexpr int BUF_OFF_T = BUF_OFF_PZ + 6 * PZH * 4;
+constexpr int BUF_OFF_PZ = BUF_OFF_PX + (6 * PXW * 4 + 127) / 128 * 128;
+constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
 constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
 constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
 constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
 constexpr int PAL_OFF_B = 2 * BUF_BYTES;
 constexpr size_t PAL_SMEM = PAL_OFF_B + 64;
-constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4;
+// every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
+constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
 static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
 static_assert((PV_FLOATS * 4) % 128 == 0 && (PS_FLOATS * 4) % 128 == 0, "TMA smem alignment");
-static_assert(BUF_OFF_PX % 16 == 0 && BUF_OFF_PZ % 16 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
-              "cp.async destinations");
-static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 4 == 0 && PAL_SMEM <= 232448, "shared memory budget");
+static_assert(BUF_OFF_PX % 128 == 0 && BUF_OFF_PZ % 128 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
+              "TMA and bulk-copy destinations");
+static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 16 == 0 && IW >= 12 + 4 + 64 && PAL_SMEM <= 232448,
+              "16-byte box rows; the id box covers x0-4 .. x0+63 from any 16-byte start; shared memory budget");
 // state slots in shared memory; after the stress phase they hold its outputs
 enum { PS_G11 = 0, PS_G22, PS_XI1, PS_XI2, PS_SXZ };
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
@@ -426,19 +444,6 @@ static_assert(sizeof(ItemMeta) <= 128, "item parameters fit their slot");
 static_assert(PCT == 32 * 2 * ((QZ + 4) / ROWS) && (QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT / 32 > 2 * (QZ / ROWS),
               "stress bands cover the 36 stress rows; velocity bands the 32 tile rows, with warps left for receivers");
 
-__device__ __forceinline__ void cp_async4(void *dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-// the mbarrier's current phase also waits for this thread's earlier cp.async copies
-__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar)
-{
-    asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 // add bytes to the current phase's transaction count without arriving
 __device__ __forceinline__ void mbar_expect_tx_only(uint64_t *bar, uint32_t bytes)
 {
@@ -545,9 +550,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             // what the fills below need from the model, read now: past the wait
             // (a compiler barrier) a batch item's descriptor would be re-read from
             // global memory on the copies' critical path
-            const uint8_t *m_ids = m.ids;
-            const float *m_px = m.px, *m_pz = m.pz, *m_mtab = m.mtab;
-            const int m_R = m.R, m_nmat = m.nmat;
+            const void *m_tmi = m.tm_ids, *m_tmx = m.tm_px, *m_tmz = m.tm_pz;
+            const float *m_mtab = m.mtab;
+            const int m_nmat = m.nmat;
             // batch items: this lane's words of the model descriptor, read now
             constexpr int MDW = (int)(sizeof(ModelDev) / 4);
             static_assert(MDW <= 64, "two descriptor words per producer lane");
@@ -567,43 +572,29 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 // the 5 state planes with a 2-row halo (bytes announced, no arrival yet)
                 float *sv = reinterpret_cast<float *>(buf);
                 float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
-                mbar_expect_tx_only(&full[b], PAL_TX_BYTES);
+                const uint32_t tab_bytes = MULTI ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
+                mbar_expect_tx_only(&full[b], PAL_TX_BYTES + tab_bytes);
                 for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, tm_v, x0, z0, cv + SF_VX + f, &full[b]);
                 tma_load_3d(ss + PS_G11 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
                 tma_load_3d(ss + PS_G22 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
                 tma_load_3d(ss + PS_XI1 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
                 tma_load_3d(ss + PS_XI2 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
                 tma_load_3d(ss + PS_SXZ * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+                // ids from padded column x0 (grid x0-4) rounded down to 16 bytes,
+                // rows from padded z0+2 (grid z0-2); profile slices from padded
+                // x0 / z0 (grid x0-4 / z0-4), all 6 rows
+                tma_load_2d(buf + BUF_OFF_I, m_tmi, x0 & ~15, z0 + 2, &full[b]);
+                tma_load_2d(buf + BUF_OFF_PX, m_tmx, x0, 0, &full[b]);
+                tma_load_2d(buf + BUF_OFF_PZ, m_tmz, z0, 0, &full[b]);
+                if (MULTI) bulk_load(buf + BUF_OFF_T, m_mtab, tab_bytes, &full[b]);
             }
-            // ids, profile slices and the material table: cp.async, tracked by full[b]
-            {
-                const unsigned char *src = m_ids + (int64_t)(z0 + 2) * P + x0;
-                unsigned char *dst = buf + BUF_OFF_I;
-                for (int i = lane; i < IH * (IW / 4); i += 32) {
-                    const int r = i / (IW / 4), c = i - r * (IW / 4);
-                    cp_async4(dst + 4 * i, src + (int64_t)r * P + 4 * c);
-                }
-                float *px = reinterpret_cast<float *>(buf + BUF_OFF_PX);
-                float *pz = reinterpret_cast<float *>(buf + BUF_OFF_PZ);
-                for (int i = lane; i < 6 * (PXW / 4); i += 32) {
-                    const int r = i / (PXW / 4), c = i - r * (PXW / 4);
-                    cp_async16(px + r * PXW + 4 * c, m_px + (int64_t)r * P + x0 + 4 * c);
-                }
-                for (int i = lane; i < 6 * (PZH / 4); i += 32) {
-                    const int r = i / (PZH / 4), c = i - r * (PZH / 4);
-                    cp_async16(pz + r * PZH + 4 * c, m_pz + (int64_t)r * m_R + z0 + 4 * c);
-                }
-                if (MULTI) {
-                    float *t = reinterpret_cast<float *>(buf + BUF_OFF_T);
-                    for (int i = lane; i < m_nmat * (MT_W / 4); i += 32) cp_async16(t + 4 * i, m_mtab + 4 * i);
-                    // the model descriptor itself, for the compute warps
-                    uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
-                    if (lane < MDW) mdst[lane] = md0;
-                    if (lane + 32 < MDW) mdst[lane + 32] = md1;
-                }
-                cp_async_mbar_arrive(&full[b]);
+            if (MULTI) {
+                // the model descriptor, for the compute warps
+                uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
+                if (lane < MDW) mdst[lane] = md0;
+                if (lane + 32 < MDW) mdst[lane + 32] = md1;
             }
-            // every lane's cp.async tracking is on full[b] before lane 0's arrival,
+            // every lane's descriptor words are written before lane 0's arrival,
             // the phase's only one, can complete it
             __syncwarp();
             if (lane == 0) {
@@ -662,7 +653,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         const float pacc = IM.pacc;
         float *sv = reinterpret_cast<float *>(buf);                 // 4 x 40 x 68, from (x0-4, z0-4)
         float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);     // 5 x 36 x 68, from (x0-4, z0-2)
-        const uint8_t *si = buf + BUF_OFF_I;                         // 37 x 68,     from (x0-4, z0-2)
+        const uint8_t *si = buf + BUF_OFF_I + (x0 & 15);            // 37 x 80,     from (x0-4, z0-2)
 
         // Interior tiles (no grid edge, C-PML strip or source within the tile
         // and its halo) take a copy of the code with every guard constant-true.
