@@ -370,14 +370,14 @@ bool encode_2d(CUtensorMap *out, CUtensorMapDataType type, void *base, int64_t d
 }
 
 // TMA descriptor of a stack of float planes (pitch P, R rows, nplanes) with a
-// (box_w x box_h x 1) box
-bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes, int box_w, int box_h)
+// (box_w x box_h x box_d) box: box_d consecutive planes in one copy
+bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes, int box_w, int box_h, int box_d)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[3] = {(cuuint64_t)m.P, (cuuint64_t)m.R, (cuuint64_t)nplanes};
     cuuint64_t strides[2] = {(cuuint64_t)m.P * 4, (cuuint64_t)m.plane * 4};
-    cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+    cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, (cuuint32_t)box_d};
     cuuint32_t es[3] = {1, 1, 1};
     return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -635,8 +635,10 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     s.f[1] = s.f[0] + NSF * m.plane;
     if (ctx->ids) {
         CUtensorMap tm[2];
-        if (!encode_planes(&tm[0], s.f[0], m, 2 * NSF, TMA_VW, TMA_VH) ||
-            !encode_planes(&tm[1], s.f[0], m, 2 * NSF, TMA_VW, TMA_SH))
+        // the 4 velocity planes (SF_VX .. SF_WZ) and the 5 stress-state planes
+        // (SF_SXZ .. SF_XI2) of a tile, one copy each
+        if (!encode_planes(&tm[0], s.f[0], m, 2 * NSF, TMA_VW, TMA_VH, 4) ||
+            !encode_planes(&tm[1], s.f[0], m, 2 * NSF, TMA_VW, TMA_SH, 5))
             return bad(cudaErrorInvalidValue, "TMA descriptor");
         if ((e = cudaMalloc(&s.tm, sizeof(tm))) != cudaSuccess) return bad(e, "TMA descriptor");
         if ((e = cudaMemcpyAsync(s.tm, tm, sizeof(tm), cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)

@@ -402,10 +402,10 @@ constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
 constexpr int IW = PAL_IDS_W, IH = PAL_IDS_H;      // ids: rows z0-2 .. z0+34; column x0-4 at (x0 & 15)
 constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
 constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
-constexpr int PS_FLOATS = (PS_BOX + 31) / 32 * 32; // slot stride: 128-B aligned TMA destinations
+constexpr int PS_FLOATS = PS_BOX;                  // slot stride: the 5 slots are one dense TMA box
 constexpr int PXW = TMA_VW, PZH = TMA_VH;          // profile slices: x0-4 .. x0+63, z0-4 .. z0+35
 constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
-constexpr int BUF_OFF_I = BUF_OFF_S + 5 * PS_FLOATS * 4;
+constexpr int BUF_OFF_I = (BUF_OFF_S + 5 * PS_FLOATS * 4 + 127) / 128 * 128;
 constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
 constexpr int BUF_OFF_PZ = BUF_OFF_PX + (6 * PXW * 4 + 127) / 128 * 128;
 constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
@@ -417,13 +417,17 @@ constexpr size_t PAL_SMEM = PAL_OFF_B + 64;
 // every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
 constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
 static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
-static_assert((PV_FLOATS * 4) % 128 == 0 && (PS_FLOATS * 4) % 128 == 0, "TMA smem alignment");
+static_assert(BUF_OFF_I % 128 == 0, "TMA smem alignment");
 static_assert(BUF_OFF_PX % 128 == 0 && BUF_OFF_PZ % 128 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
               "TMA and bulk-copy destinations");
 static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 16 == 0 && IW >= 12 + 4 + 64 && PAL_SMEM <= 232448,
               "16-byte box rows; the id box covers x0-4 .. x0+63 from any 16-byte start; shared memory budget");
 // state slots in shared memory; after the stress phase they hold its outputs
-enum { PS_G11 = 0, PS_G22, PS_XI1, PS_XI2, PS_SXZ };
+// (the planes SF_SXZ .. SF_XI2 in order: one TMA box of depth 5 fills them)
+enum { PS_SXZ = 0, PS_G11, PS_G22, PS_XI1, PS_XI2 };
+static_assert(SF_VX + 1 == SF_VZ && SF_VZ + 1 == SF_WX && SF_WX + 1 == SF_WZ && SF_SXZ + 1 == SF_G11 &&
+                  SF_G11 + 1 == SF_G22 && SF_G22 + 1 == SF_XI1 && SF_XI1 + 1 == SF_XI2,
+              "velocity planes and stress-state planes are consecutive in the state array");
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
 
 // what the producer resolves for one item (shared memory, per buffer)
@@ -569,17 +573,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             unsigned char *buf = smp + b * BUF_BYTES;
             if (lane == 0) {
                 // the big copies first: the 4 velocity planes with a 4-cell halo and
-                // the 5 state planes with a 2-row halo (bytes announced, no arrival yet)
-                float *sv = reinterpret_cast<float *>(buf);
-                float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);
+                // the 5 state planes with a 2-row halo, one box each (bytes
+                // announced, no arrival yet)
                 const uint32_t tab_bytes = MULTI ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
                 mbar_expect_tx_only(&full[b], PAL_TX_BYTES + tab_bytes);
-                for (int f = 0; f < 4; ++f) tma_load_3d(sv + f * PV_FLOATS, tm_v, x0, z0, cv + SF_VX + f, &full[b]);
-                tma_load_3d(ss + PS_G11 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G11, &full[b]);
-                tma_load_3d(ss + PS_G22 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_G22, &full[b]);
-                tma_load_3d(ss + PS_XI1 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI1, &full[b]);
-                tma_load_3d(ss + PS_XI2 * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_XI2, &full[b]);
-                tma_load_3d(ss + PS_SXZ * PS_FLOATS, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
+                tma_load_3d(buf, tm_v, x0, z0, cv + SF_VX, &full[b]);
+                tma_load_3d(buf + BUF_OFF_S, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
                 // ids from padded column x0 (grid x0-4) rounded down to 16 bytes,
                 // rows from padded z0+2 (grid z0-2); profile slices from padded
                 // x0 / z0 (grid x0-4 / z0-4), all 6 rows
