@@ -384,9 +384,11 @@ k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
 // work list of (model, shot, tile) items.  A producer warp runs one item
 // ahead: it resolves the item's model and shot (a chain of dependent global
 // loads that would otherwise stall every warp at each item), writes the
-// item's parameters to shared memory, and fills the free buffer: TMA for the
-// 4 velocity and 5 state planes with halos, cp.async for the material ids,
-// the C-PML profile slices and the material table.  Eighteen compute warps
+// item's parameters to shared memory, and fills the free buffer with five TMA
+// copies (the 4 velocity planes and the 5 state planes with halos, one box
+// each; the material ids; the two C-PML profile slices) and, for a batch item,
+// a bulk copy of its material table.  Each copy costs the producer about 120
+// cycles to issue, so the copies are few and large.  Eighteen compute warps
 // compute the item from the other buffer: a warp works 32 consecutive
 // columns (conflict-free shared-memory rows) of a band of 4 consecutive rows,
 // so the z-stencils of a column reuse the values of the rows before them in
