@@ -77,6 +77,7 @@ SYMBOLS = {
     "poe_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
     "poe_get_derived_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _fp]),
+    "poe_wait_limit_check": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "poe_checkpoint_size": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "poe_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),

@@ -787,6 +787,22 @@ int poe_get_derived_noalloc(poe_ctx *ctx, int32_t shot, int32_t field, float *ho
     return device_status(ctx);
 }
 
+int poe_wait_limit_check(int32_t device, int32_t polls, int32_t *gave_up)
+{
+    if (!gave_up || polls < 1 || polls > (1 << 24)) return POE_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return POE_ECUDA;
+    int *err = nullptr;
+    int flag = 0;
+    cudaError_t e = cudaMalloc(&err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+    if (e == cudaSuccess) e = (cudaError_t)launch_wait_limit(err, polls, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(err);
+    if (e != cudaSuccess) return POE_ECUDA;
+    *gave_up = flag;
+    return POE_OK;
+}
+
 int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_in)
 {
     ShotHost *s = get_shot(ctx, shot);

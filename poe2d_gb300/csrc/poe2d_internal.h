@@ -120,6 +120,9 @@ int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, c
                       bool exact, bool kone, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
+// one thread waits, polls times at most, on an mbarrier no thread arrives at;
+// sets *err when the wait gives up
+int launch_wait_limit(int *err, int polls, void *stream);
 // palette kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
 // columns = tile + 2-cell halo each side); TMA boxes of 68 x 40 (velocity) and
 // 68 x 36 (stress state) floats

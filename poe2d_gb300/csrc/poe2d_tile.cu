@@ -80,13 +80,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// bounded wait for a phase; false if it did not complete within the limit
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// bounded wait for a phase: false if it did not complete within `polls`
+// polls (each poll may suspend the thread for a short, system-dependent time)
+__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, int polls)
 {
-    for (int i = 0; i < (1 << 20); ++i)
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// the kernels' waits: 2^20 polls, far beyond any wait of a working step
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_n(bar, parity, 1 << 20); }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0, int c1, uint64_t *bar)
 {
@@ -976,6 +979,25 @@ int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, c
                            : batch_impl<true, false>(models_dev, shots_dev, items, nitems, k, st);
     return kone ? batch_impl<false, true>(models_dev, shots_dev, items, nitems, k, st)
                 : batch_impl<false, false>(models_dev, shots_dev, items, nitems, k, st);
+}
+
+// the bounded wait on a phase that never completes (no thread arrives): the
+// waiting thread gives up after `polls` polls, flags the error and returns
+__global__ void k_wait_limit(int *err, int polls)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_n(&bar, 0, polls)) atomicExch(err, 1);
+}
+
+int launch_wait_limit(int *err, int polls, void *stream)
+{
+    k_wait_limit<<<1, 32, 0, (cudaStream_t)stream>>>(err, polls);
+    return (int)cudaGetLastError();
 }
 
 __global__ void k_advance_shots(const StreamShot *shots, int nshots, int64_t by)

@@ -113,6 +113,14 @@ def ref_receivers(g, isource, jsource, panj, panj2, a0_pos, a1_pos):
     return np.array([(arr[i].ix, arr[i].iz, arr[i].comp) for i in range(n)], np.int32)
 
 
+def wait_limit_check(polls=1000, device=0):
+    """Run the kernels' bounded mbarrier wait against a barrier nothing arrives
+    at (poe_wait_limit_check): True when the wait gave up at its limit."""
+    out = C.c_int32(0)
+    check(L.lib().poe_wait_limit_check(int(device), int(polls), C.byref(out)))
+    return out.value == 1
+
+
 class Solver:
     """One model on the current CUDA device, with any number of shots.
 
