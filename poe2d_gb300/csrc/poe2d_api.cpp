@@ -196,9 +196,9 @@ int sync_shots(poe_ctx *ctx)
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
     }
-    // palette kernel work list: every tile of every shot, in the context's order
+    // step kernel work list: every tile of every shot, in the context's order
     ctx->items.clear();
-    if (ctx->ids) {
+    {
         auto add = [&](int i, int tx, int tz) { ctx->items.push_back(make_int4(0, i, tx * PAL_TX, tz * PAL_TZ)); };
         if (ctx->order == POE_ORDER_TILE_MAJOR) {        // the same tile of every shot side by side
             for (int tz = 0; tz < ctx->ntz; ++tz)
@@ -547,11 +547,13 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("upload: ") + cudaGetErrorString(e));
     }
-    if (rc == POE_OK && ctx->ids) {
-        // the palette kernel's producer fetches each tile's ids and profile
-        // slices with TMA (rows of P bytes / P floats / R floats)
+    if (rc == POE_OK) {
+        // the step kernel's producer fetches each tile's ids (palette models)
+        // and profile slices with TMA (rows of P bytes / P floats / R floats)
         CUtensorMap tm[3];
-        bool ok = encode_2d(&tm[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, ctx->ids, m.P, m.R, m.P, PAL_IDS_W, PAL_IDS_H) &&
+        std::memset(tm, 0, sizeof(tm));
+        bool ok = (!ctx->ids ||
+                   encode_2d(&tm[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, ctx->ids, m.P, m.R, m.P, PAL_IDS_W, PAL_IDS_H)) &&
                   encode_2d(&tm[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->px, m.P, 6, (int64_t)m.P * 4, TMA_VW, 6) &&
                   encode_2d(&tm[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->pz, m.R, 6, (int64_t)m.R * 4, TMA_VH, 6);
         cudaError_t e = ok ? cudaMalloc(&ctx->tm_model, sizeof(tm)) : cudaErrorInvalidValue;
@@ -569,12 +571,12 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     m.ids = ctx->ids;
     m.mtab = ctx->mtab;
     m.nmat = ctx->nmat;
-    m.tm_ids = ctx->tm_model ? (const void *)&ctx->tm_model[0] : nullptr;
+    m.tm_ids = ctx->tm_model && ctx->ids ? (const void *)&ctx->tm_model[0] : nullptr;
     m.tm_px = ctx->tm_model ? (const void *)&ctx->tm_model[1] : nullptr;
     m.tm_pz = ctx->tm_model ? (const void *)&ctx->tm_model[2] : nullptr;
-    // tile geometry of the kernel this model runs on (receiver lists are per tile)
-    ctx->tile_x = ctx->ids ? PAL_TX : TILE_X;
-    ctx->tile_z = ctx->ids ? PAL_TZ : TILE_Z;
+    // tile geometry of the step kernel (receiver lists are per tile)
+    ctx->tile_x = PAL_TX;
+    ctx->tile_z = PAL_TZ;
     ctx->ntx = (nx + ctx->tile_x - 1) / ctx->tile_x;
     ctx->ntz = (nz + ctx->tile_z - 1) / ctx->tile_z;
     ctx->m.ntx = ctx->ntx;
@@ -633,7 +635,7 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     if ((e = cudaMalloc(&s.f[0], 2 * fbytes)) != cudaSuccess) return bad(e, "state");
     if ((e = cudaMemsetAsync(s.f[0], 0, 2 * fbytes, ctx->stream)) != cudaSuccess) return bad(e, "state");
     s.f[1] = s.f[0] + NSF * m.plane;
-    if (ctx->ids) {
+    {
         CUtensorMap tm[2];
         // the 4 velocity planes (SF_VX .. SF_WZ) and the 5 stress-state planes
         // (SF_SXZ .. SF_XI2) of a tile, one copy each

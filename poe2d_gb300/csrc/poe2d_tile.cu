@@ -435,6 +435,21 @@ static_assert(SF_VX + 1 == SF_VZ && SF_VZ + 1 == SF_WX && SF_WX + 1 == SF_WZ && 
               "velocity planes and stress-state planes are consecutive in the state array");
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
 
+// new w and v of one cell from its coefficient planes (c at the cell, planes
+// pl apart), with the reference's float operations in its order (cu:293-311,
+// 330-353): co = (rho m - rhof^2)/dt, c1,2 = co +- rho (eta/kappa)/2
+__device__ __forceinline__ void velocity_coef(const float *__restrict__ c, int64_t pl, float dt, float A, float B,
+                                              float w0, float v0, float &w1, float &v1)
+{
+    const float rho = c[C_RHO * pl], rhof = c[C_RHOF * pl];
+    const float rsm = c[C_RSM * pl], eok = c[C_EOK * pl];
+    const float co = (rho * rsm - rhof * rhof) / dt;
+    const float c1 = co + rho * eok * 0.5f;
+    const float c2 = co - rho * eok * 0.5f;
+    w1 = (c2 * w0 + (-rhof * A - rho * B)) / c1;
+    v1 = v0 + (rsm * A + rhof * B + rhof * eok * ((w0 + w1) * 0.5f)) / co;
+}
+
 // what the producer resolves for one item (shared memory, per buffer)
 struct ItemMeta {
     float *FB;                 // state buffer written by this step
@@ -484,11 +499,12 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 }
 }  // namespace
 
-template <bool EXACT, bool KONE, bool MULTI>
+template <bool EXACT, bool KONE, bool MULTI, bool COEF>
 __global__ void __launch_bounds__(PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
            const int4 *__restrict__ items, int nitems, int k)
 {
+    static_assert(!(COEF && MULTI), "batches run palette models");
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     uint64_t *empty = full + 2;
@@ -581,13 +597,13 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 // the 5 state planes with a 2-row halo, one box each (bytes
                 // announced, no arrival yet)
                 const uint32_t tab_bytes = MULTI ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
-                mbar_expect_tx_only(&full[b], PAL_TX_BYTES + tab_bytes);
+                mbar_expect_tx_only(&full[b], PAL_TX_BYTES - (COEF ? (uint32_t)(IW * IH) : 0u) + tab_bytes);
                 tma_load_3d(buf, tm_v, x0, z0, cv + SF_VX, &full[b]);
                 tma_load_3d(buf + BUF_OFF_S, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
                 // ids from padded column x0 (grid x0-4) rounded down to 16 bytes,
                 // rows from padded z0+2 (grid z0-2); profile slices from padded
                 // x0 / z0 (grid x0-4 / z0-4), all 6 rows
-                tma_load_2d(buf + BUF_OFF_I, m_tmi, x0 & ~15, z0 + 2, &full[b]);
+                if (!COEF) tma_load_2d(buf + BUF_OFF_I, m_tmi, x0 & ~15, z0 + 2, &full[b]);
                 tma_load_2d(buf + BUF_OFF_PX, m_tmx, x0, 0, &full[b]);
                 tma_load_2d(buf + BUF_OFF_PZ, m_tmz, z0, 0, &full[b]);
                 if (MULTI) bulk_load(buf + BUF_OFF_T, m_mtab, tab_bytes, &full[b]);
@@ -641,6 +657,8 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         const Div24 qx = m.qx, qz = m.qz;
         const ItemMeta &IM = *reinterpret_cast<const ItemMeta *>(buf + BUF_OFF_M);
         const float *st = reinterpret_cast<const float *>(MULTI ? buf + BUF_OFF_T : smp + BUF_OFF_T);
+        // COEF: the 8 coefficient planes, read per cell (padded like the state: zero outside the grid)
+        const float *__restrict__ cf = m.coef;
         const float *PXs = reinterpret_cast<const float *>(buf + BUF_OFF_PX);
         const float *PZs = reinterpret_cast<const float *>(buf + BUF_OFF_PZ);
         const int NX = m.NX, NZ = m.NZ;
@@ -663,6 +681,16 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         // and its halo) take a copy of the code with every guard constant-true.
         auto compute = [&](auto interior_tag) -> bool {
             constexpr bool IN = decltype(interior_tag)::value;
+            if (COEF && lx < QX && wid < 2 * (QZ / ROWS)) {
+                // the density coefficients this thread's velocity rows read (rows
+                // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
+                const float *c = cf + (int64_t)(z0 + zb0 + ZH) * P + x0 + lx + XH;
+#pragma unroll
+                for (int i = 0; i < ROWS + 1; ++i)
+#pragma unroll
+                    for (int pl = C_RHO; pl <= C_EOK; ++pl)
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(c + pl * PL + (int64_t)i * P));
+            }
             // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
             {
                 const int x = x0 - 2 + lx;
@@ -690,7 +718,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     vxc[i] = VXc[(zb0 + 1 + i) * TMA_VW];
                 }
 #pragma unroll
-                for (int i = 0; i < ROWS + 1; ++i) idc[i] = si[(zb0 + i) * IW + lx + 2];
+                for (int i = 0; i < ROWS + 1; ++i) idc[i] = COEF ? 0 : si[(zb0 + i) * IW + lx + 2];
 #pragma unroll
                 for (int r = 0; r < ROWS; ++r) {
                     const int zl = zb0 + r;
@@ -714,9 +742,22 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
                     float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
                     float sxz = ss[PS_SXZ * PS_FLOATS + so];
-                    const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * idc[r]);
-                    const float mu_top = st[MT_W * idc[r + 1] + MT_MU];   // rmu[top] (cu:218)
-                    const float lc = ma.x, mu = ma.y, al = ma.z, M = ma.w;
+                    float lc, mu, al, M, mu_top;
+                    if (COEF) {
+                        const float *c = cf + o;
+                        lc = c[C_LC * PL];
+                        mu = c[C_MU * PL];
+                        al = c[C_AL * PL];
+                        M = c[C_M * PL];
+                        mu_top = c[C_MU * PL + P];                   // rmu[top] (cu:218)
+                    } else {
+                        const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * idc[r]);
+                        mu_top = st[MT_W * idc[r + 1] + MT_MU];      // rmu[top] (cu:218)
+                        lc = ma.x;
+                        mu = ma.y;
+                        al = ma.z;
+                        M = ma.w;
+                    }
                     const int zr = (!IN && z_ok) ? zrow(m, z) : -1;
                     float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
                     if (xc >= 0 && (g1 || g2)) {
@@ -820,7 +861,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ppc[i] = PPc[(zb0 + 1 + i) * TMA_VW];
                 }
 #pragma unroll
-                for (int i = 0; i < ROWS + 1; ++i) idc[i] = si[(zb0 + 2 + i) * IW + lx + 4];
+                for (int i = 0; i < ROWS + 1; ++i) idc[i] = COEF ? 0 : si[(zb0 + 2 + i) * IW + lx + 4];
 #pragma unroll
                 for (int r = 0; r < ROWS; ++r) {
                     const int zl = zb0 + r;
@@ -866,26 +907,36 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo], Kzh = KONE ? 1.0f : PZs[PKH * PZH + pzo];
                     float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
                     {   // vx, wx, material at (x, t) (cu:293-311)
-                        const float *mt = st + MT_W * idc[r];
-                        const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
-                        const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
-                        const float rco = mt[MT_RCO];
                         const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
                         const float B = KDIV<KONE>(d2x, Kx) + m2;
-                        const float w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                        const float v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
+                        float w1, v1;
+                        if (COEF)
+                            velocity_coef(cf + o, PL, dt, A, B, wx0, vx0, w1, v1);
+                        else {
+                            const float *mt = st + MT_W * idc[r];
+                            const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
+                            const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
+                            const float rco = mt[MT_RCO];
+                            w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                            v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
+                        }
                         if (gvx) { wx1 = w1; vx1 = v1; }
                     }
                     {   // vz, wz, material at (x, t+1) (cu:330-353)
-                        const float *mt = st + MT_W * idc[r + 1];
-                        const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
-                        const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
-                        const float rco = mt[MT_RCO];
                         float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
                         const float B = KDIV<KONE>(d3z, Kzh) + m6;
                         if (!IN && o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
-                        const float w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                        const float v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
+                        float w1, v1;
+                        if (COEF)
+                            velocity_coef(cf + o + P, PL, dt, A, B, wz0, vz0, w1, v1);
+                        else {
+                            const float *mt = st + MT_W * idc[r + 1];
+                            const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
+                            const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
+                            const float rco = mt[MT_RCO];
+                            w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
+                            v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
+                        }
                         if (gvz) { wz1 = w1; vz1 = v1; }
                     }
                     FB[SF_VX * PL + o] = vx1;
@@ -929,18 +980,16 @@ int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_tile<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TILE_SMEM);
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
         attr = true;
     }
-    if (m.ids) {
-        const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
-        if (grid > 0) k_tile_pal<EXACT, KONE, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
-    } else {
-        const int ntx = (m.NX + 1 + TX - 1) / TX, ntz = (m.NZ + 1 + TZ - 1) / TZ;
-        k_tile<EXACT, KONE><<<dim3(ntx * ntz, nshots), NT, TILE_SMEM, st>>>(m, shots, k, ntx);
+    const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
+    if (grid > 0) {
+        if (m.ids) k_tile_pal<EXACT, KONE, false, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
+        else k_tile_pal<EXACT, KONE, false, true><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
     }
     return (int)cudaGetLastError();
 }
@@ -950,13 +999,13 @@ int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *item
 {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
         attr = true;
     }
     const int grid = nitems < sm_count() ? nitems : sm_count();
     ModelDev dummy{};
-    if (grid > 0) k_tile_pal<EXACT, KONE, true><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    if (grid > 0) k_tile_pal<EXACT, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
     return (int)cudaGetLastError();
 }
 }  // namespace
