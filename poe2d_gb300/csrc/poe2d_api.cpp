@@ -74,7 +74,7 @@ struct poe_ctx {
     int ntx = 1, ntz = 1;       // tiles across x and z
     int order = 0;              // work-list order (POE_ORDER_*)
     int graph_steps = kGraphSteps;   // steps per captured graph
-    int tile_x = TILE_X, tile_z = TILE_Z;
+    int tile_x = PAL_TX, tile_z = PAL_TZ;
     std::string err;
 };
 
@@ -473,8 +473,9 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     ModelDev &m = ctx->m;
     m.NX = grid->NX;
     m.NZ = grid->NZ;
-    // tiles read columns x0-4 .. x0+TX+3 and rows z0-4 .. z0+TZ+3 of their halo;
-    // size the padded planes for both tile shapes (palette 60x32, planes 64x32)
+    // tiles (60 x 32) read columns x0-4 .. x0+63 and rows z0-4 .. z0+35; the
+    // pitch also rounds the grid up to 64-cell tiles (the 2001-cell benchmark
+    // rows: 2080 floats, not a power of two)
     {
         const int px1 = ((nx + TILE_X - 1) / TILE_X) * TILE_X + 8;
         const int px2 = ((nx + PAL_TX - 1) / PAL_TX) * PAL_TX + 8;

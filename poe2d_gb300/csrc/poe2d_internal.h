@@ -81,8 +81,10 @@ __host__ __device__ __forceinline__ int zrow(const ModelDev &m, int z)
 }
 
 // ---- fused tile step (poe2d_tile.cu) ----
-constexpr int TILE_X = 64;   // cells per tile along x
-constexpr int TILE_Z = 32;   // cells per tile along z
+// the padded planes also round the grid up to 64 x 32 cells (a layout choice
+// kept from an earlier tile shape; the step kernel's tiles are PAL_TX x PAL_TZ)
+constexpr int TILE_X = 64;
+constexpr int TILE_Z = 32;
 
 // integrated state planes per buffer (sigma_xx, sigma_zz, p are derived)
 enum { SF_VX = 0, SF_VZ, SF_WX, SF_WZ, SF_SXZ, SF_G11, SF_G22, SF_XI1, SF_XI2, NSF };

@@ -1,19 +1,19 @@
 // poe2d_tile.cu -- the fused time step: one launch = stress + velocity.
 //
-// One CTA (256 threads) advances a TX x TZ = 64 x 32 tile of one shot:
-//   1. vx vz wx wz of the tile + 4-cell halo (72 x 40) -> shared memory
-//      (16-byte vector loads, rows 16-B aligned by the padded layout);
-//   2. stress on the tile + 2-cell halo (68 x 36 cells): strains, fluid
-//      content, sigma2 = p, sigma_xz, sigma_xx, sigma_zz (cu:49-112,
-//      202-229, 231-244) -> shared memory; the integrated state of the tile's
-//      own cells -> HBM.  The halo is recomputed so no tile waits for another;
-//   3. receivers of the tile are recorded (before the velocity update, as
-//      save1_kernel runs, cu:1629);
-//   4. velocity on the tile (cu:279-386) -> HBM.
-// sigma_xx, sigma_zz and p never touch HBM.  Tiles re-read this step's inputs
-// in their halos, so the state is double-buffered: step n reads buffer
-// (n-1)&1 and writes buffer n&1 (the stress C-PML memory too; the velocity
-// C-PML memory is per-cell private and updated in place).
+// k_tile_pal: a persistent, warp-specialised kernel (one CTA per SM) walks a
+// work list of 60 x 32 tiles of any number of shots (and, for batches, of
+// models).  Per tile: stress on the tile + 2-cell halo (64 x 36 cells):
+// strains, fluid content, sigma2 = p, sigma_xz, sigma_xx, sigma_zz (cu:49-112,
+// 202-229, 231-244) -> shared memory, the integrated state of the tile's own
+// cells -> HBM; the tile's receivers (before the velocity update, as
+// save1_kernel runs, cu:1629); velocity on the tile (cu:279-386) -> HBM.  The
+// halo is recomputed so no tile waits for another.  sigma_xx, sigma_zz and p
+// never touch HBM.  Tiles re-read this step's inputs in their halos, so the
+// state is double-buffered: step n reads buffer (n-1)&1 and writes buffer n&1
+// (the stress C-PML memory too; the velocity C-PML memory is per-cell private
+// and updated in place).  Coefficients come from a material palette (one byte
+// per cell, a table row per material) or, for models with more distinct
+// materials, per cell from the 8 coefficient planes (COEF).
 //
 // Arithmetic per cell is the reference's, in the same order, with its FP64
 // sub-expressions rounded as in poe2d_math.cuh (EXACT) or plain FP32
@@ -28,22 +28,6 @@
 namespace poe {
 
 namespace {
-
-constexpr int TX = TILE_X, TZ = TILE_Z;
-constexpr int VW = TX + 8, VH = TZ + 8;     // velocity tile with halo
-constexpr int SW = TX + 4, SH = TZ + 4;     // stress tile with halo
-constexpr int NT = 256;
-#ifndef STRESS_UNROLL
-#define STRESS_UNROLL 2
-#endif
-#ifndef VEL_UNROLL
-#define VEL_UNROLL 2
-#endif
-constexpr int kStressUnroll = STRESS_UNROLL;   // cells in flight per thread (memory-level parallelism)
-constexpr int kVelUnroll = VEL_UNROLL;
-constexpr int V_FLOATS = VW * VH, S_FLOATS = SW * SH;
-enum { SV_VX = 0, SV_VZ, SV_WX, SV_WZ };
-enum { SS_SXX = 0, SS_SZZ, SS_SXZ, SS_P };
 
 template <bool EXACT>
 __device__ __forceinline__ float D4(float a, float b, float c, float d, const Div24 &q)
@@ -126,256 +110,6 @@ __device__ __forceinline__ float div_by(float a, float b, float y)
 }
 
 }  // namespace
-
-template <bool EXACT, bool KONE>
-__global__ void __launch_bounds__(NT, 2)
-k_tile(const ModelDev m, const StreamShot *__restrict__ shots, int k, int ntx)
-{
-    extern __shared__ __align__(16) float sm[];
-    float *sv = sm;                       // 4 x VH x VW
-    float *ss = sm + 4 * V_FLOATS;        // 4 x SH x SW
-    const int tid = threadIdx.x;
-    const int tx = blockIdx.x % ntx, tz = blockIdx.x / ntx;
-    const StreamShot &S = shots[blockIdx.y];
-    const int64_t n = *S.step + k + 1;
-    const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
-    const int NX = m.NX, NZ = m.NZ;
-    const int P = m.P;
-    const int64_t PL = m.plane;
-    const int x0 = tx * TX, z0 = tz * TZ;
-    const float dt = m.dt;
-    const float *__restrict__ FA = S.f[rd];
-    float *__restrict__ FB = S.f[wr];
-    const float *__restrict__ C = m.coef;
-    const float *__restrict__ PX = m.px;
-    const float *__restrict__ PZ = m.pz;
-    const int R = m.R;
-    const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
-    const int src_off = (int)S.src_off;
-    const int src_where = S.src_where;
-    const bool src_on = n <= S.src_n;
-    const float src_val = src_on ? S.src_tab[n - 1] : 0.0f;
-
-    // ---- 1. velocity tile with halo: columns x0-4 .. x0+TX+3, rows z0-4 .. z0+TZ+3.
-    //         Column x0-4 sits at padded index x0 (XH = 4): 16-B aligned rows.
-    {
-        const int vec_per_row = VW / 4;                  // 18 float4 per row
-        const int total = 4 * VH * vec_per_row;
-#pragma unroll 4
-        for (int i = tid; i < total; i += NT) {
-            const int f = i / (VH * vec_per_row);
-            const int rem = i - f * (VH * vec_per_row);
-            const int zz = rem / vec_per_row, xv = rem - zz * vec_per_row;
-            const float4 v = *reinterpret_cast<const float4 *>(
-                FA + (int64_t)(SF_VX + f) * PL + (int64_t)(z0 - 4 + zz + ZH) * P + x0 + 4 * xv);
-            *reinterpret_cast<float4 *>(sv + f * V_FLOATS + zz * VW + 4 * xv) = v;
-        }
-    }
-    __syncthreads();
-
-    // ---- 2. stress on the tile + 2-cell halo
-    const float pacc = S.acc[rd];
-#pragma unroll kStressUnroll
-    for (int i = tid; i < S_FLOATS; i += NT) {
-        const int zl = i / SW, xl = i - zl * SW;
-        const int x = x0 - 2 + xl, z = z0 - 2 + zl;
-        const int a = xl + 2, b = zl + 2;                 // position in the velocity tile
-        const float *VXs = sv + SV_VX * V_FLOATS + b * VW + a;
-        const float *VZs = sv + SV_VZ * V_FLOATS + b * VW + a;
-        const float *WXs = sv + SV_WX * V_FLOATS + b * VW + a;
-        const float *WZs = sv + SV_WZ * V_FLOATS + b * VW + a;
-        const bool cell_ok = x >= 0 && x <= NX && z >= 0 && z <= NZ;
-        const bool g1 = cell_ok && x >= 1 && x <= NX - 1 && z >= 2 && z <= NZ - 2;   // cu:60-62
-        const bool g2 = cell_ok && x >= 2 && x <= NX - 1 && z >= 1 && z <= NZ - 2;   // cu:212-214
-        const bool g3 = cell_ok && x >= 1 && x <= NX - 2 && z >= 2 && z <= NZ - 1;   // cu:237-239
-        const bool own = cell_ok && x >= x0 && x < x0 + TX && z >= z0 && z < z0 + TZ;
-        const int o = (z + ZH) * P + (x + XH);
-        // the six stencils (cu:64-65, 76-77, 220-221)
-        const float vdx = D4<EXACT>(VXs[1], VXs[0], VXs[2], VXs[-1], m.qx);
-        const float vdz = D4<EXACT>(VZs[0], VZs[-VW], VZs[VW], VZs[-2 * VW], m.qz);
-        const float wdx = D4<EXACT>(WXs[1], WXs[0], WXs[2], WXs[-1], m.qx);
-        const float wdz = D4<EXACT>(WZs[0], WZs[-VW], WZs[VW], WZs[-2 * VW], m.qz);
-        const float sdx = D4<EXACT>(VZs[0], VZs[-1], VZs[1], VZs[-2], m.qx);
-        const float sdz = D4<EXACT>(VXs[VW], VXs[0], VXs[2 * VW], VXs[-VW], m.qz);
-        float g11 = 0.0f, g22 = 0.0f, xi1 = 0.0f, xi2 = 0.0f, sxz = 0.0f;
-        float lc = 0.0f, mu = 0.0f, mu_top = 0.0f, al = 0.0f, M = 0.0f;
-        if (cell_ok) {
-            g11 = FA[SF_G11 * PL + o];
-            g22 = FA[SF_G22 * PL + o];
-            xi1 = FA[SF_XI1 * PL + o];
-            xi2 = FA[SF_XI2 * PL + o];
-            sxz = FA[SF_SXZ * PL + o];
-            lc = C[C_LC * PL + o];
-            mu = C[C_MU * PL + o];
-            mu_top = C[C_MU * PL + o + P];               // rmu[top] (cu:218)
-            al = C[C_AL * PL + o];
-            M = C[C_M * PL + o];
-        }
-        const int xc = cell_ok ? xcol(m, x) : -1;
-        const int zr = cell_ok ? zrow(m, z) : -1;
-        const int xi = x + XH, zi = z + ZH;
-        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-        if (xc >= 0 && (g1 || g2)) {
-            const int ix = z * Wx + xc;
-            const float *MA = S.mx[rd];
-            const float bxh = PX[PBH * P + xi], axh = PX[PAH * P + xi];
-            m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
-            m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
-            m5 = PX[PB * P + xi] * MA[MXS_SXZ * nzx + ix] + PX[PA * P + xi] * sdx;
-            if (own) {
-                float *MB = S.mx[wr];
-                if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
-                if (g2) MB[MXS_SXZ * nzx + ix] = m5;
-            }
-        }
-        if (zr >= 0 && (g1 || g2)) {
-            const int iz = zr * P + xi;
-            const float *MA = S.mz[rd];
-            const float bz = PZ[PB * R + zi], az = PZ[PA * R + zi];
-            m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
-            m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-            m6 = PZ[PBH * R + zi] * MA[MZS_SXZ * hzp + iz] + PZ[PAH * R + zi] * sdz;
-            if (own) {
-                float *MB = S.mz[wr];
-                if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
-                if (g2) MB[MZS_SXZ * hzp + iz] = m6;
-            }
-        }
-        const float Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-        const float Kx = KONE ? 1.0f : PX[PK * P + xi];
-        const float Kz = KONE ? 1.0f : PZ[PK * R + zi];
-        if (g1) {   // cu:71-86
-            g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
-            g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
-            xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
-            xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
-        }
-        float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
-        const bool is_src = cell_ok && o == src_off;
-        if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
-        if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-        if (is_src && own) S.acc[wr] = pv;
-        if (g2) {   // cu:223-226
-            const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
-            sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
-        }
-        float sxx = 0.0f, szz = 0.0f;
-        if (g3) {   // cu:241-242
-            if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
-            else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
-        }
-        ss[SS_SXX * S_FLOATS + i] = sxx;
-        ss[SS_SZZ * S_FLOATS + i] = szz;
-        ss[SS_SXZ * S_FLOATS + i] = sxz;
-        ss[SS_P * S_FLOATS + i] = pv;
-        if (own) {
-            FB[SF_G11 * PL + o] = g11;
-            FB[SF_G22 * PL + o] = g22;
-            FB[SF_XI1 * PL + o] = xi1;
-            FB[SF_XI2 * PL + o] = xi2;
-            FB[SF_SXZ * PL + o] = sxz;
-        }
-    }
-    __syncthreads();
-
-    // ---- 3. receivers of this tile (vx, vz before the update; p of this step)
-    if (S.nrec > 0 && n <= S.trace_cap) {
-        const int tile = tz * ntx + tx;
-        const int qb = S.rec_start[tile], qe = S.rec_start[tile + 1];
-        float *trace_row = S.trace + (n - 1) * S.nrec;
-        for (int q = qb + tid; q < qe; q += NT) {
-            const int4 Rq = S.rec_sorted[q];             // (x, comp, slot, z)
-            const int xl = Rq.x - x0, zl = Rq.w - z0;
-            float v;
-            if (Rq.y == 2) v = ss[SS_P * S_FLOATS + (zl + 2) * SW + xl + 2];
-            else v = sv[(Rq.y == 0 ? SV_VX : SV_VZ) * V_FLOATS + (zl + 4) * VW + xl + 4];
-            trace_row[Rq.z] = v;
-        }
-    }
-
-    // ---- 4. velocity on the tile
-    float *__restrict__ MXV = S.mxv;
-    float *__restrict__ MZV = S.mzv;
-#pragma unroll kVelUnroll
-    for (int i = tid; i < TX * TZ; i += NT) {
-        const int zl = i / TX, xl = i - zl * TX;
-        const int x = x0 + xl, t = z0 + zl;
-        if (x > NX || t > NZ) continue;
-        const int c = xl + 2, d = zl + 2;                // position in the stress tile
-        const float *SXX = ss + SS_SXX * S_FLOATS + d * SW + c;
-        const float *SZZ = ss + SS_SZZ * S_FLOATS + d * SW + c;
-        const float *SXZ = ss + SS_SXZ * S_FLOATS + d * SW + c;
-        const float *PP = ss + SS_P * S_FLOATS + d * SW + c;
-        const int vo = (zl + 4) * VW + xl + 4;
-        const float vx0 = sv[SV_VX * V_FLOATS + vo], vz0 = sv[SV_VZ * V_FLOATS + vo];
-        const float wx0 = sv[SV_WX * V_FLOATS + vo], wz0 = sv[SV_WZ * V_FLOATS + vo];
-        const int o = (t + ZH) * P + (x + XH);
-        const int xi = x + XH, zi = t + ZH;
-        // the six stencils (cu:297-299, 342-344)
-        const float d1x = D4<EXACT>(SXX[0], SXX[-1], SXX[1], SXX[-2], m.qx);
-        const float d2x = D4<EXACT>(PP[0], PP[-1], PP[1], PP[-2], m.qx);
-        const float d3x = D4<EXACT>(SXZ[0], SXZ[-SW], SXZ[SW], SXZ[-2 * SW], m.qz);
-        const float d1z = D4<EXACT>(SXZ[1], SXZ[0], SXZ[2], SXZ[-1], m.qx);
-        const float d2z = D4<EXACT>(SZZ[SW], SZZ[0], SZZ[2 * SW], SZZ[-SW], m.qz);
-        const float d3z = D4<EXACT>(PP[SW], PP[0], PP[2 * SW], PP[-SW], m.qz);
-        const bool gvx = x >= 2 && x <= NX - 1 && t >= 2 && t <= NZ - 1;   // cu:289-291
-        const bool gvz = x >= 1 && x <= NX - 2 && t >= 1 && t <= NZ - 2;   // cu:326-328
-        const int xc = xcol(m, x), zr = zrow(m, t);
-        float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-        if (xc >= 0 && (gvx || gvz)) {
-            const int ix = t * Wx + xc;
-            float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix, *M4 = MXV + MXV_VZ * nzx + ix;
-            const float bx = PX[PB * P + xi], ax = PX[PA * P + xi];
-            m1 = bx * *M1 + ax * d1x;
-            m2 = bx * *M2 + ax * d2x;
-            m4 = PX[PBH * P + xi] * *M4 + PX[PAH * P + xi] * d1z;
-            if (gvx) { *M1 = m1; *M2 = m2; }
-            if (gvz) *M4 = m4;
-        }
-        if (zr >= 0 && (gvx || gvz)) {
-            const int iz = zr * P + xi;
-            float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz, *M6 = MZV + MZV_VZ2 * hzp + iz;
-            const float bh = PZ[PBH * R + zi], ah = PZ[PAH * R + zi];
-            m3 = PZ[PB * R + zi] * *M3 + PZ[PA * R + zi] * d3x;
-            m5 = bh * *M5 + ah * d2z;
-            m6 = bh * *M6 + ah * d3z;
-            if (gvx) *M3 = m3;
-            if (gvz) { *M5 = m5; *M6 = m6; }
-        }
-        const float Kx = KONE ? 1.0f : PX[PK * P + xi], Kxh = KONE ? 1.0f : PX[PKH * P + xi];
-        const float Kz = KONE ? 1.0f : PZ[PK * R + zi], Kzh = KONE ? 1.0f : PZ[PKH * R + zi];
-        float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
-        if (gvx) {   // material at (x, t), cu:293-311
-            const float rho = C[C_RHO * PL + o], rhof = C[C_RHOF * PL + o];
-            const float rsm = C[C_RSM * PL + o], eok = C[C_EOK * PL + o];
-            const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
-            const float B = KDIV<KONE>(d2x, Kx) + m2;
-            const float co = (rho * rsm - rhof * rhof) / dt;
-            const float c1 = co + rho * eok * 0.5f;
-            const float c2 = co - rho * eok * 0.5f;
-            wx1 = (c2 * wx0 + (-rhof * A - rho * B)) / c1;
-            vx1 = vx0 + (rsm * A + rhof * B + rhof * eok * ((wx0 + wx1) * 0.5f)) / co;
-        }
-        if (gvz) {   // material at (x, t+1), cu:330-353
-            const int op = o + P;
-            const float rho = C[C_RHO * PL + op], rhof = C[C_RHOF * PL + op];
-            const float rsm = C[C_RSM * PL + op], eok = C[C_EOK * PL + op];
-            float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
-            const float B = KDIV<KONE>(d3z, Kzh) + m6;
-            if (o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
-            const float co = (rho * rsm - rhof * rhof) / dt;
-            const float c1 = co + rho * eok * 0.5f;
-            const float c2 = co - rho * eok * 0.5f;
-            wz1 = (c2 * wz0 + (-rhof * A - rho * B)) / c1;
-            vz1 = vz0 + (rsm * A + rhof * B + rhof * eok * ((wz0 + wz1) * 0.5f)) / co;
-        }
-        FB[SF_VX * PL + o] = vx1;
-        FB[SF_WX * PL + o] = wx1;
-        FB[SF_VZ * PL + o] = vz1;
-        FB[SF_WZ * PL + o] = wz1;
-    }
-}
-
 
 // ===================================================================== palette
 // Same step as k_tile for models whose 8 coefficient planes take at most
@@ -971,15 +705,12 @@ int sm_count()
     return sms;
 }
 
-constexpr size_t TILE_SMEM = sizeof(float) * (4 * V_FLOATS + 4 * S_FLOATS);
-
 template <bool EXACT, bool KONE>
 int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4 *items, int nitems, int k,
               cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_tile<EXACT, KONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TILE_SMEM);
         cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
         cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
