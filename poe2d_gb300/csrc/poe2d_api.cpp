@@ -143,15 +143,6 @@ void strips(const float *prof, int n1, int &lo, int &hi)
     }
 }
 
-Div24 make_div(float h)
-{
-    Div24 q;
-    const double D = 24.0 * (double)h;
-    q.D = (float)D;
-    q.exact_tie = ((double)q.D == D) ? 1 : 0;
-    q.inv = (float)(1.0 / D);
-    return q;
-}
 
 int sync_shots(poe_ctx *ctx)
 {
@@ -484,8 +475,8 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     }
     m.plane = (int64_t)m.P * m.R;
     m.dt = grid->dt;
-    m.qx = make_div(grid->dx);
-    m.qz = make_div(grid->dz);
+    m.qx = make_div24(grid->dx);
+    m.qz = make_div24(grid->dz);
     strips(prof_x, nx, m.xL, m.xR);
     strips(prof_z, nz, m.zT, m.zB);
     m.Wx = m.xL + (nx - m.xR);
@@ -1141,7 +1132,7 @@ struct poe_batch {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int device = 0;
-    bool exact = true, kone = true;
+    bool exact = true, kone = true, few = true;
     ModelDev *models_dev = nullptr;
     StreamShot *shots_dev = nullptr;
     int4 *items_dev = nullptr;
@@ -1193,7 +1184,7 @@ int grow(poe_batch *b, T **p, int &cap, int need)
 int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
 {
     for (int64_t k = 0; k < nsteps; ++k) {
-        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->kone,
+        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->few, b->kone,
                                         b->stream);
         if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
     }
@@ -1211,7 +1202,7 @@ cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
     int rc = 0;
     for (int k = 0; k < kGraphSteps && rc == 0; ++k)
-        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->kone, b->stream);
+        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->few, b->kone, b->stream);
     if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -1263,6 +1254,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
     b->device = ctxs[0]->device;
     b->exact = ctxs[0]->exact;
     for (poe_ctx *c : b->ctxs) b->kone = b->kone && c->kone;   // K = 1 divides are exact: KONE=false is safe
+    for (poe_ctx *c : b->ctxs) b->few = b->few && c->m.qx.few_bits && c->m.qz.few_bits;
     if (cudaSetDevice(b->device) != cudaSuccess) {
         delete b;
         return POE_ECUDA;

@@ -29,10 +29,15 @@ namespace poe {
 
 namespace {
 
-template <bool EXACT>
+// stencil modes: plain FP32, and the reference's FP64 rounding for a spacing
+// whose 24 h is a float of few bits (0.5, 1, 1.25, ...) or for any spacing
+enum { SM_FAST = 0, SM_EXACT_FEW = 1, SM_EXACT_ANY = 2 };
+
+template <int SM>
 __device__ __forceinline__ float D4(float a, float b, float c, float d, const Div24 &q)
 {
-    return EXACT ? d4_exact(a, b, c, d, q) : d4_fast(a, b, c, d, q);
+    return SM == SM_FAST ? d4_fast(a, b, c, d, q)
+                         : (SM == SM_EXACT_FEW ? d4_exact_few(a, b, c, d, q) : d4_exact_any(a, b, c, d, q));
 }
 
 template <bool KONE>
@@ -233,11 +238,12 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 }
 }  // namespace
 
-template <bool EXACT, bool KONE, bool MULTI, bool COEF>
+template <int SM, bool KONE, bool MULTI, bool COEF>
 __global__ void __launch_bounds__(PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
            const int4 *__restrict__ items, int nitems, int k)
 {
+    constexpr bool EXACT = SM != SM_FAST;
     static_assert(!(COEF && MULTI), "batches run palette models");
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
@@ -467,12 +473,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const bool g3 = IN || (cell_ok && x_g3 && z >= 2 && z <= NZ - 1);   // cu:237-239
                     const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
                     const int o = (z + ZH) * P + xi;
-                    const float vdx = D4<EXACT>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], qx);
-                    const float vdz = D4<EXACT>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], qz);
-                    const float wdx = D4<EXACT>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], qx);
-                    const float wdz = D4<EXACT>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], qz);
-                    const float sdx = D4<EXACT>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], qx);
-                    const float sdz = D4<EXACT>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], qz);
+                    const float vdx = D4<SM>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], qx);
+                    const float vdz = D4<SM>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], qz);
+                    const float wdx = D4<SM>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], qx);
+                    const float wdz = D4<SM>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], qz);
+                    const float sdx = D4<SM>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], qx);
+                    const float sdz = D4<SM>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], qz);
                     float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
                     float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
                     float sxz = ss[PS_SXZ * PS_FLOATS + so];
@@ -607,12 +613,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
                     const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
                     const int o = (t + ZH) * P + xi;
-                    const float d1x = D4<EXACT>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], qx);
-                    const float d2x = D4<EXACT>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], qx);
-                    const float d3x = D4<EXACT>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], qz);
-                    const float d1z = D4<EXACT>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], qx);
-                    const float d2z = D4<EXACT>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], qz);
-                    const float d3z = D4<EXACT>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], qz);
+                    const float d1x = D4<SM>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], qx);
+                    const float d2x = D4<SM>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], qx);
+                    const float d3x = D4<SM>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], qz);
+                    const float d1z = D4<SM>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], qx);
+                    const float d2z = D4<SM>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], qz);
+                    const float d3z = D4<SM>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], qz);
                     const bool gvx = IN || (x_vx && t >= 2 && t <= NZ - 1);   // cu:289-291
                     const bool gvz = IN || (x_vz && t >= 1 && t <= NZ - 2);   // cu:326-328
                     const int zr = IN ? -1 : zrow(m, t);
@@ -705,60 +711,74 @@ int sm_count()
     return sms;
 }
 
-template <bool EXACT, bool KONE>
+template <int SM, bool KONE>
 int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4 *items, int nitems, int k,
               cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<SM, KONE, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<SM, KONE, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
         attr = true;
     }
     const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
     if (grid > 0) {
-        if (m.ids) k_tile_pal<EXACT, KONE, false, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
-        else k_tile_pal<EXACT, KONE, false, true><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
+        if (m.ids) k_tile_pal<SM, KONE, false, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
+        else k_tile_pal<SM, KONE, false, true><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
     }
     return (int)cudaGetLastError();
 }
 
-template <bool EXACT, bool KONE>
+template <int SM, bool KONE>
 int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems, int k, cudaStream_t st)
 {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_tile_pal<EXACT, KONE, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_tile_pal<SM, KONE, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)PAL_SMEM);
         attr = true;
     }
     const int grid = nitems < sm_count() ? nitems : sm_count();
     ModelDev dummy{};
-    if (grid > 0) k_tile_pal<EXACT, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    if (grid > 0) k_tile_pal<SM, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
     return (int)cudaGetLastError();
 }
 }  // namespace
+
+// the stencil mode of a launch: FAST, or EXACT for the spacings of its models
+static int stencil_mode(bool exact, bool few)
+{
+    return !exact ? SM_FAST : (few ? SM_EXACT_FEW : SM_EXACT_ANY);
+}
 
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
                      bool exact, bool kone, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (exact) return kone ? tile_impl<true, true>(m, shots_dev, nshots, items, nitems, k, st)
-                           : tile_impl<true, false>(m, shots_dev, nshots, items, nitems, k, st);
-    return kone ? tile_impl<false, true>(m, shots_dev, nshots, items, nitems, k, st)
-                : tile_impl<false, false>(m, shots_dev, nshots, items, nitems, k, st);
+    switch (stencil_mode(exact, m.qx.few_bits && m.qz.few_bits) * 2 + (kone ? 1 : 0)) {
+    case 0: return tile_impl<SM_FAST, false>(m, shots_dev, nshots, items, nitems, k, st);
+    case 1: return tile_impl<SM_FAST, true>(m, shots_dev, nshots, items, nitems, k, st);
+    case 2: return tile_impl<SM_EXACT_FEW, false>(m, shots_dev, nshots, items, nitems, k, st);
+    case 3: return tile_impl<SM_EXACT_FEW, true>(m, shots_dev, nshots, items, nitems, k, st);
+    case 4: return tile_impl<SM_EXACT_ANY, false>(m, shots_dev, nshots, items, nitems, k, st);
+    default: return tile_impl<SM_EXACT_ANY, true>(m, shots_dev, nshots, items, nitems, k, st);
+    }
 }
 
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool kone, void *stream)
+                      bool exact, bool exact_few, bool kone, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
-    if (exact) return kone ? batch_impl<true, true>(models_dev, shots_dev, items, nitems, k, st)
-                           : batch_impl<true, false>(models_dev, shots_dev, items, nitems, k, st);
-    return kone ? batch_impl<false, true>(models_dev, shots_dev, items, nitems, k, st)
-                : batch_impl<false, false>(models_dev, shots_dev, items, nitems, k, st);
+    switch (stencil_mode(exact, exact_few) * 2 + (kone ? 1 : 0)) {
+    case 0: return batch_impl<SM_FAST, false>(models_dev, shots_dev, items, nitems, k, st);
+    case 1: return batch_impl<SM_FAST, true>(models_dev, shots_dev, items, nitems, k, st);
+    case 2: return batch_impl<SM_EXACT_FEW, false>(models_dev, shots_dev, items, nitems, k, st);
+    case 3: return batch_impl<SM_EXACT_FEW, true>(models_dev, shots_dev, items, nitems, k, st);
+    case 4: return batch_impl<SM_EXACT_ANY, false>(models_dev, shots_dev, items, nitems, k, st);
+    default: return batch_impl<SM_EXACT_ANY, true>(models_dev, shots_dev, items, nitems, k, st);
+    }
 }
 
 // the bounded wait on a phase that never completes (no thread arrives): the

@@ -20,12 +20,12 @@ def _materials(poe, n, seed):
     return out
 
 
-def _case(poe, oracle_mod, NX, NZ, nmat, kmax, src_xz, fast, n=90, seed=0):
+def _case(poe, oracle_mod, NX, NZ, nmat, kmax, src_xz, fast, n=90, seed=0, h=0.5):
     O = oracle_mod
     rng = np.random.default_rng(seed)
     ids = rng.integers(0, nmat, size=(NZ + 1, NX + 1)).astype(np.uint8)
     coef, vp = poe.coeffs_biot(_materials(poe, nmat, seed), ids)
-    g = poe.grid(NX, NZ, 0.5, 4e-5)
+    g = poe.grid(NX, NZ, h, 4e-5 * h / 0.5)
     par = poe.pml_defaults(min(8, NX // 4, NZ // 4), 200.0, vp)
     par.k_max = kmax
     px, pz = poe.pml_profiles(g, params=par)
@@ -39,9 +39,9 @@ def _case(poe, oracle_mod, NX, NZ, nmat, kmax, src_xz, fast, n=90, seed=0):
             out[pal] = [s.traces(), s.field("vz"), s.field("p"), s.field("sxz")]
     for a, b in zip(out[True], out[False]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
-    o = O.Oracle(O.F32 if fast else O.REFMIXED, NX, NZ, 0.5, 0.5, 4e-5, coef, px, pz)
-    o.set_source(src_xz[0], src_xz[1], O.SRC_FZ, O.source_table(1, 200.0, 4e-5, n, amplitude=1e3, t_cut=0.0,
-                                                                  dx=0.5, dz=0.5))
+    o = O.Oracle(O.F32 if fast else O.REFMIXED, NX, NZ, g.dx, g.dz, g.dt, coef, px, pz)
+    o.set_source(src_xz[0], src_xz[1], O.SRC_FZ, O.source_table(1, 200.0, g.dt, n, amplitude=1e3, t_cut=0.0,
+                                                                  dx=g.dx, dz=g.dz))
     o.set_receivers(rec)
     ref = o.run(n)
     tol = 1e-5 if fast else 1e-6
@@ -89,3 +89,11 @@ def test_force_source_on_column_zero_excites_nothing(poe, palette):
         s.run(60)
         assert not s.traces().any()
         assert not s.field("vz").any() and not s.field("p").any()
+
+
+@pytest.mark.parametrize("h", [0.3, 0.1])
+def test_exact_stencils_at_spacings_whose_24h_has_many_bits(poe, oracle_mod, h):
+    """24 h = 7.2 or 2.4 (26 bits for 0.1): the stencil division keeps a float
+    quotient only where its rounding is certain and takes the reference's FP64
+    line elsewhere, so EXACT follows the oracle's FP64 stencils here too."""
+    _case(poe, oracle_mod, 119, 63, 3, 1.0, (60, 31), False, h=h)
