@@ -117,10 +117,11 @@ __device__ __forceinline__ float div_by(float a, float b, float y)
 }  // namespace
 
 // ===================================================================== palette
-// Same step as k_tile for models whose 8 coefficient planes take at most
-// MAX_PALETTE distinct values (patchy models: 2): each cell carries a one-byte
-// material id and every per-cell coefficient the reference computes (co, c1,
-// c2, rhof*eta/kappa, 1/co, 1/c1) comes from a table row in shared memory.
+// For models whose 8 coefficient planes take at most MAX_PALETTE distinct
+// values (patchy models: 2) each cell carries a one-byte material id and every
+// per-cell coefficient the reference computes (co, c1, c2, rhof*eta/kappa,
+// 1/co, 1/c1) comes from a table row in shared memory; other models (COEF)
+// read the 8 coefficient planes per cell.
 //
 // Persistent, warp-specialised and double-buffered: one CTA per SM walks the
 // work list of (model, shot, tile) items.  A producer warp runs one item

@@ -1,8 +1,9 @@
 """Palette kernel at the edges of its geometry: grids smaller than one tile,
 grids that are exact tile multiples (60 x 32 cells), the 64-material limit,
 a C-PML with K != 1 on the single-model kernel, and sources next to the
-grid's edges.  Each case must equal the coefficient-plane kernel bit for bit
-and the oracle within the stencil mode's tolerance."""
+grid's edges.  Each case must equal the same model read from its 8
+coefficient planes (palette=False) bit for bit, and the oracle within the
+stencil mode's tolerance."""
 import numpy as np
 import pytest
 

@@ -131,8 +131,9 @@ def _patchy(poe, NX, NZ, seed):
 @pytest.mark.parametrize("fast", [False, True])
 def test_palette_path_matches_planes_and_oracle(poe, oracle_mod, fast):
     """A two-material patchy model runs on the palette kernel (one byte per
-    cell, TMA-staged tiles); the same model with palette=False runs on the
-    coefficient-plane kernel.  Both must agree bit for bit, and with the oracle."""
+    cell, TMA-staged tiles); the same model with palette=False reads its 8
+    coefficient planes per cell (COEF).  Both must agree bit for bit, and with
+    the oracle."""
     O = oracle_mod
     # 251 x 201 with a 10-cell C-PML: most 60 x 32 tiles are interior (no
     # edge, strip or source), the rest take the guarded path
