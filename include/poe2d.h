@@ -267,8 +267,9 @@ void poe_destroy(poe_ctx *ctx);
 /* A batch advances the shots of several contexts (models of any sizes) in one
  * persistent launch per time step: no reference counterpart (the reference
  * runs one shot of one model per process, cu:1596-1736).  Every context must
- * be on the same device, use the material palette (few distinct materials, no
- * POE_CTX_NO_PALETTE) and the same stencil mode.  The contexts stay owned by
+ * be on the same device and use the same stencil mode, and either all use the
+ * material palette (few distinct materials) or none does (per-cell
+ * coefficient planes: many materials or POE_CTX_NO_PALETTE).  The contexts stay owned by
  * the caller and must outlive the batch; a context belongs to at most one
  * batch at a time.  stream: a cudaStream_t or NULL for a private stream. */
 typedef struct poe_batch poe_batch;

@@ -1133,6 +1133,7 @@ struct poe_batch {
     bool own_stream = false;
     int device = 0;
     bool exact = true, kone = true, few = true;
+    bool coef = false;          // the models read their coefficient planes per cell
     ModelDev *models_dev = nullptr;
     StreamShot *shots_dev = nullptr;
     int4 *items_dev = nullptr;
@@ -1184,7 +1185,7 @@ int grow(poe_batch *b, T **p, int &cap, int need)
 int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
 {
     for (int64_t k = 0; k < nsteps; ++k) {
-        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->few, b->kone,
+        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->few, b->coef, b->kone,
                                         b->stream);
         if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
     }
@@ -1202,7 +1203,7 @@ cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
     int rc = 0;
     for (int k = 0; k < kGraphSteps && rc == 0; ++k)
-        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->few, b->kone, b->stream);
+        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->few, b->coef, b->kone, b->stream);
     if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -1243,7 +1244,8 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
     if (!ctxs || n <= 0) return POE_EINVAL;
     for (int i = 0; i < n; ++i) {
         if (!ctxs[i]) return POE_EINVAL;
-        if (!ctxs[i]->ids) return fail(ctxs[i], POE_EINVAL, "batch: context without a material palette");
+        if ((ctxs[i]->ids == nullptr) != (ctxs[0]->ids == nullptr))
+            return fail(ctxs[i], POE_EINVAL, "batch: palette models and per-cell coefficient models in one batch");
         if (ctxs[i]->device != ctxs[0]->device) return fail(ctxs[i], POE_EINVAL, "batch: contexts on other devices");
         if (ctxs[i]->exact != ctxs[0]->exact) return fail(ctxs[i], POE_EINVAL, "batch: mixed stencil modes");
         for (int j = 0; j < i; ++j)
@@ -1253,6 +1255,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
     b->ctxs.assign(ctxs, ctxs + n);
     b->device = ctxs[0]->device;
     b->exact = ctxs[0]->exact;
+    b->coef = ctxs[0]->ids == nullptr;
     for (poe_ctx *c : b->ctxs) b->kone = b->kone && c->kone;   // K = 1 divides are exact: KONE=false is safe
     for (poe_ctx *c : b->ctxs) b->few = b->few && c->m.qx.few_bits && c->m.qz.few_bits;
     if (cudaSetDevice(b->device) != cudaSuccess) {

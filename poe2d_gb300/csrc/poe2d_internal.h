@@ -117,10 +117,11 @@ struct StreamShot {
 // of (0, shot, x0, z0)
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
                      bool exact, bool kone, void *stream);
-// one step over several palette models: items (model, shot, x0, z0) index models_dev and shots_dev;
-// exact_few: every model's spacings have a 24 h of few bits
+// one step over several models: items (model, shot, x0, z0) index models_dev and shots_dev;
+// exact_few: every model's spacings have a 24 h of few bits; coef: the models read
+// their 8 coefficient planes per cell (all of them), else each has a material palette
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool exact_few, bool kone, void *stream);
+                      bool exact, bool exact_few, bool coef, bool kone, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
 // one thread waits, polls times at most, on an mbarrier no thread arrives at;

@@ -23,6 +23,7 @@
 #include <mutex>
 #include <type_traits>
 
+#include "launch_attr.h"
 #include "poe2d_internal.h"
 
 namespace poe {
@@ -245,7 +246,6 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
            const int4 *__restrict__ items, int nitems, int k)
 {
     constexpr bool EXACT = SM != SM_FAST;
-    static_assert(!(COEF && MULTI), "batches run palette models");
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     uint64_t *empty = full + 2;
@@ -337,7 +337,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 // the big copies first: the 4 velocity planes with a 4-cell halo and
                 // the 5 state planes with a 2-row halo, one box each (bytes
                 // announced, no arrival yet)
-                const uint32_t tab_bytes = MULTI ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
+                const uint32_t tab_bytes = (MULTI && !COEF) ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
                 mbar_expect_tx_only(&full[b], PAL_TX_BYTES - (COEF ? (uint32_t)(IW * IH) : 0u) + tab_bytes);
                 tma_load_3d(buf, tm_v, x0, z0, cv + SF_VX, &full[b]);
                 tma_load_3d(buf + BUF_OFF_S, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
@@ -347,7 +347,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 if (!COEF) tma_load_2d(buf + BUF_OFF_I, m_tmi, x0 & ~15, z0 + 2, &full[b]);
                 tma_load_2d(buf + BUF_OFF_PX, m_tmx, x0, 0, &full[b]);
                 tma_load_2d(buf + BUF_OFF_PZ, m_tmz, z0, 0, &full[b]);
-                if (MULTI) bulk_load(buf + BUF_OFF_T, m_mtab, tab_bytes, &full[b]);
+                if (MULTI && !COEF) bulk_load(buf + BUF_OFF_T, m_mtab, tab_bytes, &full[b]);
             }
             if (MULTI) {
                 // the model descriptor, for the compute warps
@@ -700,30 +700,28 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
 }
 
 namespace {
+// SMs of the current device (the persistent grid: one CTA per SM)
 int sm_count()
 {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
+    static std::atomic<int> sms[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::atomic<int> &n = sms[dev & 63];
+    if (!n.load(std::memory_order_relaxed)) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        n.store(v > 0 ? v : 1, std::memory_order_relaxed);
     }
-    return sms;
+    return n.load(std::memory_order_relaxed);
 }
 
 template <int SM, bool KONE>
 int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4 *items, int nitems, int k,
               cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_tile_pal<SM, KONE, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PAL_SMEM);
-        cudaFuncSetAttribute(k_tile_pal<SM, KONE, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PAL_SMEM);
-        attr = true;
-    }
+    static std::atomic<uint64_t> pal_done{0}, coef_done{0};
+    smem_attr_once(k_tile_pal<SM, KONE, false, false>, (int)PAL_SMEM, pal_done);
+    smem_attr_once(k_tile_pal<SM, KONE, false, true>, (int)PAL_SMEM, coef_done);
     const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
     if (grid > 0) {
         if (m.ids) k_tile_pal<SM, KONE, false, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k);
@@ -733,17 +731,20 @@ int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4
 }
 
 template <int SM, bool KONE>
-int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems, int k, cudaStream_t st)
+int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems, int k, bool coef,
+               cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_tile_pal<SM, KONE, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)PAL_SMEM);
-        attr = true;
-    }
+    static std::atomic<uint64_t> pal_done{0}, coef_done{0};
     const int grid = nitems < sm_count() ? nitems : sm_count();
     ModelDev dummy{};
-    if (grid > 0) k_tile_pal<SM, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    if (grid <= 0) return (int)cudaGetLastError();
+    if (coef) {
+        smem_attr_once(k_tile_pal<SM, KONE, true, true>, (int)PAL_SMEM, coef_done);
+        k_tile_pal<SM, KONE, true, true><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    } else {
+        smem_attr_once(k_tile_pal<SM, KONE, true, false>, (int)PAL_SMEM, pal_done);
+        k_tile_pal<SM, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k);
+    }
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -769,16 +770,16 @@ int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots,
 }
 
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool exact_few, bool kone, void *stream)
+                      bool exact, bool exact_few, bool coef, bool kone, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
     switch (stencil_mode(exact, exact_few) * 2 + (kone ? 1 : 0)) {
-    case 0: return batch_impl<SM_FAST, false>(models_dev, shots_dev, items, nitems, k, st);
-    case 1: return batch_impl<SM_FAST, true>(models_dev, shots_dev, items, nitems, k, st);
-    case 2: return batch_impl<SM_EXACT_FEW, false>(models_dev, shots_dev, items, nitems, k, st);
-    case 3: return batch_impl<SM_EXACT_FEW, true>(models_dev, shots_dev, items, nitems, k, st);
-    case 4: return batch_impl<SM_EXACT_ANY, false>(models_dev, shots_dev, items, nitems, k, st);
-    default: return batch_impl<SM_EXACT_ANY, true>(models_dev, shots_dev, items, nitems, k, st);
+    case 0: return batch_impl<SM_FAST, false>(models_dev, shots_dev, items, nitems, k, coef, st);
+    case 1: return batch_impl<SM_FAST, true>(models_dev, shots_dev, items, nitems, k, coef, st);
+    case 2: return batch_impl<SM_EXACT_FEW, false>(models_dev, shots_dev, items, nitems, k, coef, st);
+    case 3: return batch_impl<SM_EXACT_FEW, true>(models_dev, shots_dev, items, nitems, k, coef, st);
+    case 4: return batch_impl<SM_EXACT_ANY, false>(models_dev, shots_dev, items, nitems, k, coef, st);
+    default: return batch_impl<SM_EXACT_ANY, true>(models_dev, shots_dev, items, nitems, k, coef, st);
     }
 }
 

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "launch_attr.h"
 #include "sg_internal.h"
 #include "sm103_ptx.cuh"
 
@@ -287,11 +288,8 @@ int launch(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, in
            float *ws, int *err, cudaStream_t st)
 {
     using L = GemmSmem<BN, ST>;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_gemm<BN, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL);
-        attr = true;
-    }
+    static std::atomic<uint64_t> done{0};
+    poe::smem_attr_once(k_gemm<BN, ST>, L::TOTAL, done);
     const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
     k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, M, N, K, kper, e, splits > 1 ? ws : nullptr, err);
     return (int)cudaGetLastError();

@@ -248,8 +248,8 @@ class Solver:
 class Batch:
     """Several Solvers advanced together, one persistent launch per time step.
 
-    Every solver must use the material palette (the default for patchy
-    models) and the same stencil mode.  run(steps) takes one step count per
+    Every solver must use the same stencil mode, and either all use the
+    material palette (the default for patchy models) or none does.  run(steps) takes one step count per
     solver (or one for all); each solver's shots end exactly as after
     solver.run(steps[i]).  The solvers must outlive the batch.
     """

@@ -1,9 +1,10 @@
 """Batched solver: several models of uneven sizes and step counts in one
 persistent launch per step must end exactly where separate runs end.
 
-The batch kernel is the palette kernel over a concatenated work list
+The batch kernel is the step kernel over a concatenated work list
 (model, shot, tile); each model reads its own grid, profiles and material
-table, so the comparison with single-context runs is bit for bit.
+table (or coefficient planes), so the comparison with single-context runs
+is bit for bit.
 """
 import numpy as np
 import pytest
@@ -40,9 +41,9 @@ def _build(poe, fast):
     return out
 
 
-def _solver(poe, case, fast):
+def _solver(poe, case, fast, palette=True):
     g, coef, px, pz, srcs, rec = case
-    s = poe.Solver(g, coef, px, pz, fast=fast)
+    s = poe.Solver(g, coef, px, pz, fast=fast, palette=palette)
     for src in srcs:
         s.add_shot(src, rec)
     return s
@@ -60,11 +61,12 @@ def _same(a, b):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
 
 
+@pytest.mark.parametrize("palette", [True, False])
 @pytest.mark.parametrize("fast", [False, True])
-def test_batch_matches_single_runs(poe, fast):
+def test_batch_matches_single_runs(poe, fast, palette):
     cases = _build(poe, fast)
     runs = [[150, 70, 0, 213, 64], [40, 0, 100, 64, 1]]     # uneven, with idle models and graph + tail segments
-    ref = [_solver(poe, c, fast) for c in cases]
+    ref = [_solver(poe, c, fast, palette) for c in cases]
     for r in runs:
         for i, s in enumerate(ref):
             if r[i]:
@@ -73,7 +75,7 @@ def test_batch_matches_single_runs(poe, fast):
     for s in ref:
         s.close()
 
-    solvers = [_solver(poe, c, fast) for c in cases]
+    solvers = [_solver(poe, c, fast, palette) for c in cases]
     with poe.Batch(solvers) as b:
         for r in runs:
             b.run(r)
@@ -98,7 +100,7 @@ def test_batch_rejects_mixed_contexts(poe):
     c = poe.Solver(g, coef, px, pz, palette=False)
     c.add_shot(srcs[0], rec)
     with pytest.raises(poe.PoeError):
-        poe.Batch([a, c])                     # coefficient-plane model
+        poe.Batch([a, c])                     # a palette model with a per-cell coefficient model
     with pytest.raises(poe.PoeError):
         poe.Batch([a, a])                     # listed twice
     with poe.Batch([a]) as bt:
