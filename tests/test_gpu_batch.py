@@ -108,3 +108,28 @@ def test_batch_rejects_mixed_contexts(poe):
             bt.run([-1])
     for s in (a, b, c):
         s.close()
+
+
+def test_batch_at_a_spacing_whose_24h_has_many_bits(poe):
+    """h = 0.3: the batch launches the exact-division variant for any spacing;
+    each model must end exactly where its own run ends."""
+    cases = []
+    for i, (NX, NZ) in enumerate([(90, 70), (130, 45)]):
+        coef, vp = _patchy(poe, NX, NZ, 70 + i)
+        g = poe.grid(NX, NZ, 0.3, 3e-5)
+        px, pz = poe.pml_profiles(g, 8, 200.0, vp)
+        rec = [(x, 12, c) for c in (0, 1, 2) for x in range(10, NX - 10, 9)]
+        cases.append((g, coef, px, pz, [poe.source(NX // 2, 14, poe.SRC_RICKER_FZ, 200.0, 1e3, 0.0)], rec))
+    steps = [150, 97]
+    ref = [_solver(poe, c, False) for c in cases]
+    for s, n in zip(ref, steps):
+        s.run(n)
+    want = [_state(s, 1) for s in ref]
+    solvers = [_solver(poe, c, False) for c in cases]
+    with poe.Batch(solvers) as b:
+        b.run(steps)
+        b.sync()
+    for s, w in zip(solvers, want):
+        _same(_state(s, 1), w)
+    for s in ref + solvers:
+        s.close()
