@@ -432,6 +432,46 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     for (int pl = C_RHO; pl <= C_EOK; ++pl)
                         asm volatile("prefetch.global.L1 [%0];" ::"l"(c + pl * PL + (int64_t)i * P));
             }
+            if (!IN && lx < QX && wid < 2 * (QZ / ROWS) && x0 + lx <= NX) {
+                // the velocity C-PML memory this thread updates in place after the
+                // stress phase (rows zb0 .. zb0+3 of column lx, on the strips): to L1 now
+                const int x = x0 + lx;
+                const int xc = xcol(m, x);
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int t = z0 + zb0 + r;
+                    if (t > NZ) break;
+                    const int zr = zrow(m, t);
+                    if (xc >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + t * Wx + xc));
+                    if (zr >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
+                }
+            }
+            if (!IN && x0 - 2 + lx >= 0 && x0 - 2 + lx <= NX) {
+                // the stress C-PML memory of this thread's 4 stress rows: to L1 before
+                // the first row needs it
+                const int x = x0 - 2 + lx;
+                const int xc = xcol(m, x);
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int z = z0 - 2 + zb0 + r;
+                    if (z < 0 || z > NZ) continue;
+                    const int zr = zrow(m, z);
+                    if (xc >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxr + a * nzx + z * Wx + xc));
+                    if (zr >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzr + a * hzp + zr * P + x + XH));
+                }
+            }
             // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
             {
                 const int x = x0 - 2 + lx;
