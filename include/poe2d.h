@@ -227,7 +227,7 @@ int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes);
 int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capacity);
 int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_t size);
 
-/* Tuning (no reference counterpart).  The palette kernel walks a list of
+/* Tuning (no reference counterpart).  The step kernel walks a list of
  * (shot, tile) items, one CTA per SM; the order of that list decides which
  * tiles run side by side (halo reuse in L2), and poe_run replays a captured
  * CUDA graph of graph_steps steps.  Results do not depend on either. */

@@ -53,8 +53,8 @@ struct ModelDev {
     const float *mtab;       // nmat rows of MT_W floats
     int nmat;
     int ntx;                 // tiles across x of the kernel this model runs on (receiver lists)
-    // palette mode: TMA descriptors (device memory) of the id plane and of the
-    // 6 x-profile and 6 z-profile rows, boxed for the palette kernel's tiles
+    // TMA descriptors (device memory) of the id plane (palette models only) and
+    // of the 6 x-profile and 6 z-profile rows, boxed for the step kernel's tiles
     const void *tm_ids, *tm_px, *tm_pz;
 };
 
@@ -113,8 +113,8 @@ struct StreamShot {
     const void *tm_s;
 };
 
-// one step of a model's shots; palette models take the work list items[0..nitems)
-// of (0, shot, x0, z0)
+// one step of a model's shots over the work list items[0..nitems) of
+// (0, shot, x0, z0)
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
                      bool exact, bool kone, void *stream);
 // one step over several models: items (model, shot, x0, z0) index models_dev and shots_dev;
@@ -127,7 +127,7 @@ int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, vo
 // one thread waits, polls times at most, on an mbarrier no thread arrives at;
 // sets *err when the wait gives up
 int launch_wait_limit(int *err, int polls, void *stream);
-// palette kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
+// step kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
 // columns = tile + 2-cell halo each side); TMA boxes of 68 x 40 (velocity) and
 // 68 x 36 (stress state) floats
 constexpr int PAL_TX = 60, PAL_TZ = 32;
