@@ -16,6 +16,14 @@ void d4_many(const float *a, const float *b, const float *c, const float *d, lon
     }
 }
 
+void div24_info(float h, float *D, float *Dl, int *few_bits)
+{
+    const poe::Div24 q = poe::make_div24(h);
+    *D = q.D;
+    *Dl = q.Dl;
+    *few_bits = q.few_bits;
+}
+
 void sxz_many(const float *s, const float *c33, const float *S, long n, float dt, float *out)
 {
     for (long i = 0; i < n; ++i) out[i] = poe::sxz_exact(s[i], c33[i], S[i], dt);

@@ -38,6 +38,7 @@ def harness(tmp_path_factory):
     lib = C.CDLL(out)
     lib.d4_many.argtypes = [_fp, _fp, _fp, _fp, C.c_long, C.c_float, _fp, _fp]
     lib.sxz_many.argtypes = [_fp, _fp, _fp, C.c_long, C.c_float, _fp]
+    lib.div24_info.argtypes = [C.c_float, _fp, _fp, C.POINTER(C.c_int)]
     lib.sxx_szz_many.argtypes = [_fp] * 6 + [C.c_long, _fp, _fp]
     return lib
 
@@ -135,3 +136,16 @@ def test_sxx_szz_exact_match_fp64_expressions(harness):
     ref_zz = (lg1 + (L + 2.0 * M) * G2 - ap).astype(np.float32)
     assert np.array_equal(sxx.view(np.uint32), ref_xx.view(np.uint32))
     assert np.array_equal(szz.view(np.uint32), ref_zz.view(np.uint32))
+
+
+@pytest.mark.parametrize("h, few", [(0.5, 1), (1.0, 1), (1.25, 1), (2.5, 1), (5.0, 1), (10.0, 1), (0.25, 1),
+                                    (0.1, 0), (0.3, 0), (0.7, 0), (0.2, 0), (3.3, 0)])
+def test_divisor_split_and_kind(harness, h, few):
+    """24 h = D + Dl exactly (D its float rounding, Dl the rest), and the
+    few-bit tie resolution only for a float D of at most 8 significant bits."""
+    D, Dl, fb = C.c_float(), C.c_float(), C.c_int()
+    harness.div24_info(h, C.byref(D), C.byref(Dl), C.byref(fb))
+    exact = 24.0 * float(np.float32(h))
+    assert float(D.value) + float(Dl.value) == exact
+    assert np.float32(D.value) == np.float32(exact)
+    assert fb.value == few
