@@ -105,15 +105,6 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0,
         : "memory");
 }
 
-// a / b, correctly rounded, from y = RN(1/b) (Markstein 1990: with y the
-// correctly rounded reciprocal and q0 within an ulp of a/b, the residual is
-// exact and q0 + r y rounds to RN(a/b)); valid away from overflow/underflow
-__device__ __forceinline__ float div_by(float a, float b, float y)
-{
-    const float q0 = a * y;
-    const float r = fmaf(-b, q0, a);
-    return fmaf(r, y, q0);
-}
 
 }  // namespace
 

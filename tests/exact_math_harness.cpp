@@ -16,6 +16,11 @@ void d4_many(const float *a, const float *b, const float *c, const float *d, lon
     }
 }
 
+void div_by_many(const float *a, const float *b, long n, float *out)
+{
+    for (long i = 0; i < n; ++i) out[i] = poe::div_by(a[i], b[i], 1.0f / b[i]);
+}
+
 void div24_info(float h, float *D, float *Dl, int *few_bits)
 {
     const poe::Div24 q = poe::make_div24(h);

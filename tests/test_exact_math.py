@@ -39,6 +39,7 @@ def harness(tmp_path_factory):
     lib.d4_many.argtypes = [_fp, _fp, _fp, _fp, C.c_long, C.c_float, _fp, _fp]
     lib.sxz_many.argtypes = [_fp, _fp, _fp, C.c_long, C.c_float, _fp]
     lib.div24_info.argtypes = [C.c_float, _fp, _fp, C.POINTER(C.c_int)]
+    lib.div_by_many.argtypes = [_fp, _fp, C.c_long, _fp]
     lib.sxx_szz_many.argtypes = [_fp] * 6 + [C.c_long, _fp, _fp]
     return lib
 
@@ -149,3 +150,18 @@ def test_divisor_split_and_kind(harness, h, few):
     assert float(D.value) + float(Dl.value) == exact
     assert np.float32(D.value) == np.float32(exact)
     assert fb.value == few
+
+
+def test_markstein_division_is_correctly_rounded(harness):
+    """The palette kernel divides by c1 and co with q0 = a y, r = fma(-b, q0, a),
+    q = fma(r, y, q0) and y = RN(1/b) from the material table: IEEE-rounded
+    quotients for operands away from overflow and underflow, as the
+    reference's own float divisions (cu:307-311)."""
+    rng = np.random.default_rng(5)
+    n = 4_000_000
+    a = _f32(rng.standard_normal(n) * 10.0 ** rng.uniform(-20, 20, n))
+    b = _f32(rng.uniform(1.0, 2.0, n) * 10.0 ** rng.uniform(-12, 12, n) * rng.choice([-1, 1], n))
+    out = np.empty(n, np.float32)
+    harness.div_by_many(_p(a), _p(b), n, _p(out))
+    ref = a / b                                          # numpy float32 division: IEEE round to nearest
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
