@@ -1,24 +1,25 @@
-"""FP32 drift of the benchmark configurations against an FP64 run of the
+"""FP32 drift of the benchmark workloads against an FP64 run of the
 reference loop.
 
-For each configuration the GPU runs the shot with EXACT stencils (the
-reference's FP32 storage with FP64 stencil temporaries, bit for bit) and with
-FAST stencils (plain FP32), and the oracle runs the same inputs in F64 on the
-host cores.  One JSON line per configuration gives the relative L2 error of
-the traces against F64 and the largest trace error relative to the trace peak.
+For each workload the GPU runs the shot with EXACT stencils (the reference's
+FP32 storage with FP64 stencil temporaries, bit for bit) and with FAST
+stencils (plain FP32), and the oracle runs the same inputs in F64 on the host
+cores.  One JSON line per shot gives the relative L2 error of the traces
+against F64 and the largest trace error relative to the trace peak.
 
-    python tests/fp64_drift.py                 # configurations 1-4
-    python tests/fp64_drift.py --configs 1,3   # a subset
+    python tests/fp64_drift.py                                     # all four
+    python tests/fp64_drift.py --workloads sandstone201,shots1001  # a subset
 
-Configurations (synthetic, seeded):
-  1  201 x 201 homogeneous water-saturated sandstone, 20-cell C-PML, 2000
-     steps, vertical-force Ricker at the centre, 11 receivers 40 cells above
-  2  the 2001 x 2001 patchy benchmark shot, 40-cell C-PML, 20000 steps, 400
-     surface receivers
-  3  shot 0 of the 64-shot batch: 1001 x 1001 patchy model, 30-cell C-PML,
-     10000 steps, 256 surface receivers
-  4  the first four models of the uneven batch (seed 7): side U[256, 1536],
-     steps 4 x side, 128 surface receivers each
+Workloads (synthetic, seeded):
+  sandstone201  201 x 201 homogeneous water-saturated sandstone, 20-cell
+                C-PML, 2000 steps, vertical-force Ricker at the centre, 11
+                receivers 40 cells above
+  patchy2001    the 2001 x 2001 patchy benchmark shot, 40-cell C-PML, 20000
+                steps, 400 surface receivers
+  shots1001     shot 0 of the 64-shot batch: 1001 x 1001 patchy model,
+                30-cell C-PML, 10000 steps, 256 surface receivers
+  uneven4       the first four models of the uneven batch (seed 7): side
+                U[256, 1536], steps 4 x side, 128 surface receivers each
 
 Test infrastructure: it runs the oracle (needs a CUDA device and the built
 oracle library).
@@ -47,19 +48,19 @@ def sandstone_201():
     px, pz = P.pml_profiles(g, 20, 200.0, vp)
     src = P.source(100, 100, P.SRC_RICKER_FZ, 200.0, 1e6, 0.0)
     rec = [(x, 60, c) for c in (P.REC_VX, P.REC_VZ, P.REC_P) for x in range(50, 151, 10)]
-    return [("config 1: 201^2 sandstone, 2000 steps", g, coef, px, pz, src, rec, 2000)]
+    return [("201^2 sandstone, 2000 steps", g, coef, px, pz, src, rec, 2000)]
 
 
 def benchmark_2001():
     import bench
     g, coef, px, pz, src, rec, _ = bench.workload()
-    return [("config 2: 2001^2 patchy shot, 20000 steps", g, coef, px, pz, src, rec, bench.NSTEPS)]
+    return [("2001^2 patchy shot, 20000 steps", g, coef, px, pz, src, rec, bench.NSTEPS)]
 
 
 def shots_1001():
     import bench
     g, coef, px, pz, srcs, rec = bench.shots_model(64, 1001, 30, 256)
-    return [("config 3: 1001^2 patchy model, shot 0 of 64, 10000 steps", g, coef, px, pz, srcs[0], rec, 10000)]
+    return [("1001^2 patchy model, shot 0 of 64, 10000 steps", g, coef, px, pz, srcs[0], rec, 10000)]
 
 
 def uneven_4():
@@ -67,12 +68,13 @@ def uneven_4():
     out = []
     for sp in D.uneven_specs(7, 256)[:4]:
         g, coef, px, pz, src, rec, _ = D.build_model(sp)
-        out.append(("config 4: uneven model %d, side %d, %d steps" % (sp["index"], sp["side"], sp["steps"]),
+        out.append(("uneven model %d, side %d, %d steps" % (sp["index"], sp["side"], sp["steps"]),
                     g, coef, px, pz, src, rec, sp["steps"]))
     return out
 
 
-CONFIGS = {1: sandstone_201, 2: benchmark_2001, 3: shots_1001, 4: uneven_4}
+WORKLOADS = {"sandstone201": sandstone_201, "patchy2001": benchmark_2001, "shots1001": shots_1001,
+             "uneven4": uneven_4}
 
 
 def gpu_traces(g, coef, px, pz, src, rec, nsteps, fast):
@@ -100,18 +102,18 @@ def drift(t, ref):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--configs", default="1,2,3,4")
+    ap.add_argument("--workloads", default=",".join(WORKLOADS))
     args = ap.parse_args(argv)
     from oracle import oracle as O
     O.build()
-    for c in [int(v) for v in args.configs.split(",")]:
-        for name, g, coef, px, pz, src, rec, nsteps in CONFIGS[c]():
+    for w in args.workloads.split(","):
+        for name, g, coef, px, pz, src, rec, nsteps in WORKLOADS[w]():
             t0 = time.perf_counter()
             ref = f64_traces(g, coef, px, pz, src, rec, nsteps)
             t_cpu = time.perf_counter() - t0
             ex = gpu_traces(g, coef, px, pz, src, rec, nsteps, False)
             fa = gpu_traces(g, coef, px, pz, src, rec, nsteps, True)
-            print(json.dumps({"config": name, "cells": (g.NX + 1) * (g.NZ + 1), "steps": nsteps,
+            print(json.dumps({"workload": name, "cells": (g.NX + 1) * (g.NZ + 1), "steps": nsteps,
                               "receivers": len(rec), "exact_vs_f64": drift(ex, ref), "fast_vs_f64": drift(fa, ref),
                               "fast_vs_exact": drift(fa, ex), "f64_cpu_s": round(t_cpu, 1),
                               "f64_threads": os.cpu_count()}), flush=True)
