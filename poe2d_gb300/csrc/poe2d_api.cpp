@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -149,11 +150,12 @@ int sync_shots(poe_ctx *ctx)
     if (!ctx->shots_dirty) return POE_OK;
     const int ns = (int)ctx->shots.size();
     if (ns > ctx->shots_dev_cap) {
+        const int cap = std::max(ns, 2 * ctx->shots_dev_cap);
         cudaFree(ctx->shots_dev);
         cudaFree(ctx->steps_dev);
         ctx->shots_dev = nullptr;
         ctx->steps_dev = nullptr;
-        const int cap = std::max(ns, 2 * ctx->shots_dev_cap);
+        ctx->shots_dev_cap = 0;   // a failed allocation below leaves no stale capacity
         CK(cudaMalloc(&ctx->shots_dev, sizeof(StreamShot) * cap));
         CK(cudaMalloc(&ctx->steps_dev, sizeof(int64_t) * cap));
         ctx->shots_dev_cap = cap;
@@ -207,9 +209,10 @@ int sync_shots(poe_ctx *ctx)
     }
     const int ni = (int)ctx->items.size();
     if (ni > ctx->items_dev_cap) {
+        const int cap = std::max(ni, 2 * ctx->items_dev_cap);
         cudaFree(ctx->items_dev);
         ctx->items_dev = nullptr;
-        const int cap = std::max(ni, 2 * ctx->items_dev_cap);
+        ctx->items_dev_cap = 0;
         CK(cudaMalloc(&ctx->items_dev, sizeof(int4) * cap));
         ctx->items_dev_cap = cap;
     }
@@ -236,13 +239,23 @@ int ensure_source(poe_ctx *ctx, ShotHost &s, int64_t need)
     int64_t nact = 0;
     int rc = poe_source_table(&ctx->g, &s.src, cap, tab.data(), &nact);
     if (rc != POE_OK) return fail(ctx, rc, "source table");
-    cudaFree(s.src_tab);
-    s.src_tab = nullptr;
+    // the new table replaces the old one only once it is on the device: the
+    // shots' device records keep pointing at a live table if anything fails
+    float *nt = nullptr;
     if (nact > 0) {
-        CK(cudaMalloc(&s.src_tab, sizeof(float) * nact));
-        CK(cudaMemcpyAsync(s.src_tab, tab.data(), sizeof(float) * nact, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
+        cudaError_t e = cudaMalloc(&nt, sizeof(float) * nact);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(nt, tab.data(), sizeof(float) * nact, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {
+            cudaFree(nt);
+            return fail(ctx, e == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,
+                        std::string("source table: ") + cudaGetErrorString(e));
+        }
     }
+    CK(cudaStreamSynchronize(ctx->stream));   // no launch still reads the old table
+    cudaFree(s.src_tab);
+    s.src_tab = nt;
     s.src_n = nact;
     s.src_cap = cap;
     s.src_complete = nact < cap;
@@ -256,19 +269,21 @@ int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
     const int64_t cap = std::max<int64_t>(need, std::max<int64_t>(256, s.trace_cap + s.trace_cap / 2));
     float *nt = nullptr;
     CK(cudaMalloc(&nt, sizeof(float) * cap * s.nrec));
-    CK(cudaMemsetAsync(nt, 0, sizeof(float) * cap * s.nrec, ctx->stream));
-    if (s.trace && s.trace_cap)
-        CK(cudaMemcpyAsync(nt, s.trace, sizeof(float) * s.trace_cap * s.nrec, cudaMemcpyDeviceToDevice,
-                           ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    cudaError_t e = cudaMemsetAsync(nt, 0, sizeof(float) * cap * s.nrec, ctx->stream);
+    if (e == cudaSuccess && s.trace && s.trace_cap)
+        e = cudaMemcpyAsync(nt, s.trace, sizeof(float) * s.trace_cap * s.nrec, cudaMemcpyDeviceToDevice,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {   // the shot keeps its old trace buffer
+        cudaFree(nt);
+        return fail(ctx, POE_ECUDA, std::string("trace buffer: ") + cudaGetErrorString(e));
+    }
     cudaFree(s.trace);
     s.trace = nt;
     s.trace_cap = cap;
     ctx->shots_dirty = true;
     return POE_OK;
 }
-
-int kernels_per_step(const poe_ctx *) { return 1; }
 
 int step_launch(poe_ctx *ctx, int k)
 {
@@ -281,7 +296,7 @@ int run_direct(poe_ctx *ctx, int64_t nsteps)
     const int ns = (int)ctx->shots.size();
     for (int64_t k = 0; k < nsteps; ++k) {
         CKL(step_launch(ctx, (int)k));
-        ctx->launches += kernels_per_step(ctx);
+        ctx->launches += 1;
     }
     CKL(launch_advance(ctx->steps_dev, ns, nsteps, ctx->stream));
     ctx->launches += 1;
@@ -309,7 +324,7 @@ int build_graph(poe_ctx *ctx)
         ctx->graph = nullptr;
         return fail(ctx, POE_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
-    ctx->graph_kernels = ctx->graph_steps * kernels_per_step(ctx) + 1;
+    ctx->graph_kernels = ctx->graph_steps + 1;   // one step kernel per step, one clock advance
     return POE_OK;
 }
 
@@ -333,16 +348,21 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
 
 EncodeTiledFn encode_fn()
 {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    // contexts may be created on several threads at once: the entry point is
+    // published atomically (a failed lookup is retried by the next caller)
+    static std::atomic<EncodeTiledFn> fn{nullptr};
+    EncodeTiledFn f = fn.load(std::memory_order_acquire);
+    if (!f) {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
+            q == cudaDriverEntryPointSuccess) {
+            f = (EncodeTiledFn)p;
+            fn.store(f, std::memory_order_release);
+        }
     }
-    return fn;
+    return f;
 }
 
 // TMA descriptor of a 2-D array (d0 elements per row, d1 rows, rows stride
