@@ -142,6 +142,22 @@ int poe_coeffs_from_medium(const poe_grid *grid, const float *medium, const floa
 int poe_coeffs_biot(int64_t ncell, const poe_biot_material *mats, int32_t nmat,
                     const uint8_t *ids, float *coef, float *vp_max_out);
 
+/* The material palette poe_create builds when a model's 8 coefficient planes
+ * take at most POE_MAX_MATERIALS distinct tuples (patchy models): a one-byte
+ * id per cell and one row of POE_MROW floats per material.  A row holds the 8
+ * coefficients (POE_C_* order), then what the velocity update derives from
+ * them per cell, with the reference's float operations (cu:293-295, 311):
+ * co = (rho m - rho_f^2) / dt, c1 = co + rho (eta/kappa) 0.5,
+ * c2 = co - rho (eta/kappa) 0.5, rho_f (eta/kappa); then 1/co and 1/c1,
+ * correctly rounded.  ids: ncell bytes; rows: POE_MAX_MATERIALS * POE_MROW
+ * floats.  *nmat = 0 when the model has more tuples, or a material whose co
+ * or c1 is not a normal float: poe_create then keeps the 8 coefficient planes
+ * and reads them per cell. */
+enum { POE_MAX_MATERIALS = 64, POE_MROW = 14 };
+enum { POE_M_CO = 8, POE_M_C1 = 9, POE_M_C2 = 10, POE_M_RHOF_EOK = 11, POE_M_RCO = 12, POE_M_RC1 = 13 };
+int poe_material_palette(const float *coef, int64_t ncell, float dt, uint8_t *ids, float *rows,
+                         int32_t *nmat);
+
 /* Courant checks of cu:1197-1212 (max cp dt/dx <= 1/sqrt(2) and
  * <= (6/7)/sqrt(2)).  Returns POE_OK or POE_ECFL. */
 int poe_check_courant(const poe_grid *grid, float cp_max);

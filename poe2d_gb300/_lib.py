@@ -17,6 +17,8 @@ SRC_REF_DGAUSS_P, SRC_RICKER_FZ = 0, 1
 REC_NONE, REC_VX, REC_VZ, REC_P = -1, 0, 1, 2
 CTX_FAST_STENCIL = 1
 CTX_NO_PALETTE = 2
+MAX_MATERIALS, MROW = 64, 14
+M_CO, M_C1, M_C2, M_RHOF_EOK, M_RCO, M_RC1 = range(8, 14)
 FIELDS = ["vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22", "xi1", "xi2"]
 COEFS = ["rho", "rhof", "rsm", "eok", "lambdac", "mu", "alpha", "rbm"]
 
@@ -66,6 +68,8 @@ SYMBOLS = {
     "poe_pml_defaults": (None, [C.POINTER(PmlParams), C.c_int32, C.c_float, C.c_float]),
     "poe_coeffs_from_medium": (C.c_int, [C.POINTER(Grid), _fp, _fp, _fp, _fp, _fp, C.c_int32, _fp]),
     "poe_coeffs_biot": (C.c_int, [C.c_int64, C.POINTER(BiotMaterial), C.c_int32, C.POINTER(C.c_uint8), _fp, _fp]),
+    "poe_material_palette": (C.c_int, [_fp, C.c_int64, C.c_float, C.POINTER(C.c_uint8), _fp,
+                                       C.POINTER(C.c_int32)]),
     "poe_check_courant": (C.c_int, [C.POINTER(Grid), C.c_float]),
     "poe_source_table": (C.c_int, [C.POINTER(Grid), C.POINTER(Source), C.c_int64, _fp, C.POINTER(C.c_int64)]),
     "poe_create": (C.c_int, [C.POINTER(Grid), _fp, _fp, _fp, C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p)]),

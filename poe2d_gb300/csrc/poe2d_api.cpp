@@ -19,6 +19,7 @@
 
 #include "../../include/poe2d.h"
 #include "poe2d_internal.h"
+#include "poe2d_palette.h"
 
 using namespace poe;
 
@@ -393,59 +394,6 @@ bool encode_planes(CUtensorMap *out, float *base, const ModelDev &m, int nplanes
     return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-// Palette of the coefficient planes: ids (one byte per cell) and table rows
-// holding the 8 coefficients plus what the reference derives from them per
-// cell, with the reference's float operations (cu:293-295, 311).  False if
-// there are more than MAX_PALETTE distinct cells.
-bool build_palette(const float *coef, int64_t ncell, float dt, std::vector<uint8_t> &ids, std::vector<float> &tab)
-{
-    std::vector<std::array<uint32_t, POE_NCOEF>> keys;
-    ids.resize((size_t)ncell);
-    int last = -1;
-    for (int64_t j = 0; j < ncell; ++j) {
-        std::array<uint32_t, POE_NCOEF> key;
-        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&key[c], coef + c * ncell + j, 4);
-        int id = -1;
-        if (last >= 0 && keys[last] == key) id = last;
-        for (int i = 0; id < 0 && i < (int)keys.size(); ++i)
-            if (keys[i] == key) id = i;
-        if (id < 0) {
-            if ((int)keys.size() >= MAX_PALETTE) return false;
-            keys.push_back(key);
-            id = (int)keys.size() - 1;
-        }
-        ids[(size_t)j] = (uint8_t)id;
-        last = id;
-    }
-    tab.assign(keys.size() * MT_W, 0.0f);
-    for (size_t i = 0; i < keys.size(); ++i) {
-        float *t = tab.data() + i * MT_W;
-        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&t[c], &keys[i][c], 4);
-        const float rho = t[POE_C_RHO], rhof = t[POE_C_RHOF], rsm = t[POE_C_RSM], eok = t[POE_C_EOK];
-        const float co = (rho * rsm - rhof * rhof) / dt;
-        float row[MT_W] = {0};
-        row[MT_LC] = t[POE_C_LAMBDAC];
-        row[MT_MU] = t[POE_C_MU];
-        row[MT_AL] = t[POE_C_ALPHA];
-        row[MT_M] = t[POE_C_RBM];
-        row[MT_RHO] = rho;
-        row[MT_RHOF] = rhof;
-        row[MT_RSM] = rsm;
-        row[MT_EOK] = eok;
-        row[MT_RHOF_EOK] = rhof * eok;
-        row[MT_CO] = co;
-        row[MT_C1] = co + rho * eok * 0.5f;
-        row[MT_C2] = co - rho * eok * 0.5f;
-        row[MT_RCO] = (float)(1.0 / (double)co);
-        row[MT_RC1] = (float)(1.0 / (double)row[MT_C1]);
-        std::memcpy(t, row, sizeof(row));
-        if (!std::isfinite(row[MT_RCO]) || !std::isfinite(row[MT_RC1]) || !std::isnormal(co) ||
-            !std::isnormal(row[MT_C1]))
-            return false;   // degenerate material: keep the plane path and IEEE division
-    }
-    return true;
 }
 
 ShotHost *get_shot(poe_ctx *ctx, int32_t shot)

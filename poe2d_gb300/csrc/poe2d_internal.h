@@ -26,6 +26,7 @@
 #include <stdint.h>
 
 #include "poe2d_math.cuh"
+#include "poe2d_palette.h"
 
 namespace poe {
 
@@ -58,16 +59,6 @@ struct ModelDev {
     const void *tm_ids, *tm_px, *tm_pz;
 };
 
-// material-table row: coefficients and the quantities the reference derives
-// from them per cell, rounded as it rounds them, grouped for 16-byte loads:
-//   [lambda_c mu alpha M] [c2 rhof rho c1] [1/c1 m rhof*eta/kappa co] [1/co eta/kappa - -]
-enum {
-    MT_LC = 0, MT_MU, MT_AL, MT_M,
-    MT_C2, MT_RHOF, MT_RHO, MT_C1,
-    MT_RC1, MT_RSM, MT_RHOF_EOK, MT_CO,
-    MT_RCO, MT_EOK, MT_W = 16
-};
-constexpr int MAX_PALETTE = 64;
 
 // x-strip column of x, or -1
 __host__ __device__ __forceinline__ int xcol(const ModelDev &m, int x)

@@ -5,11 +5,13 @@
 // arrays are bit-identical to what its main() computes (float variables,
 // FP64 wherever a double literal appears, the <cmath> float overloads for
 // float arguments).  Compiled with -ffp-contract=off.
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "../../include/poe2d.h"
+#include "poe2d_palette.h"
 
 namespace {
 
@@ -74,6 +76,59 @@ bool grid_ok(const poe_grid *g)
 }
 
 }  // namespace
+
+namespace poe {
+
+bool build_palette(const float *coef, int64_t ncell, float dt, std::vector<uint8_t> &ids, std::vector<float> &tab)
+{
+    std::vector<std::array<uint32_t, POE_NCOEF>> keys;
+    ids.resize((size_t)ncell);
+    int last = -1;
+    for (int64_t j = 0; j < ncell; ++j) {
+        std::array<uint32_t, POE_NCOEF> key;
+        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&key[c], coef + c * ncell + j, 4);
+        int id = -1;
+        if (last >= 0 && keys[last] == key) id = last;
+        for (int i = 0; id < 0 && i < (int)keys.size(); ++i)
+            if (keys[i] == key) id = i;
+        if (id < 0) {
+            if ((int)keys.size() >= MAX_PALETTE) return false;
+            keys.push_back(key);
+            id = (int)keys.size() - 1;
+        }
+        ids[(size_t)j] = (uint8_t)id;
+        last = id;
+    }
+    tab.assign(keys.size() * MT_W, 0.0f);
+    for (size_t i = 0; i < keys.size(); ++i) {
+        float *t = tab.data() + i * MT_W;
+        for (int c = 0; c < POE_NCOEF; ++c) std::memcpy(&t[c], &keys[i][c], 4);
+        const float rho = t[POE_C_RHO], rhof = t[POE_C_RHOF], rsm = t[POE_C_RSM], eok = t[POE_C_EOK];
+        const float co = (rho * rsm - rhof * rhof) / dt;
+        float row[MT_W] = {0};
+        row[MT_LC] = t[POE_C_LAMBDAC];
+        row[MT_MU] = t[POE_C_MU];
+        row[MT_AL] = t[POE_C_ALPHA];
+        row[MT_M] = t[POE_C_RBM];
+        row[MT_RHO] = rho;
+        row[MT_RHOF] = rhof;
+        row[MT_RSM] = rsm;
+        row[MT_EOK] = eok;
+        row[MT_RHOF_EOK] = rhof * eok;
+        row[MT_CO] = co;
+        row[MT_C1] = co + rho * eok * 0.5f;
+        row[MT_C2] = co - rho * eok * 0.5f;
+        row[MT_RCO] = (float)(1.0 / (double)co);
+        row[MT_RC1] = (float)(1.0 / (double)row[MT_C1]);
+        std::memcpy(t, row, sizeof(row));
+        if (!std::isfinite(row[MT_RCO]) || !std::isfinite(row[MT_RC1]) || !std::isnormal(co) ||
+            !std::isnormal(row[MT_C1]))
+            return false;   // degenerate material: keep the plane path and IEEE division
+    }
+    return true;
+}
+
+}  // namespace poe
 
 extern "C" {
 
@@ -254,6 +309,27 @@ int32_t poe_ref_receivers(const poe_grid *grid, int32_t isource, int32_t jsource
     const int xc = (NX + 1) / 2 - 1;                        // cu:181-200
     for (int y : {50, a0_pos, a1_pos, jsource}) put(xc, y, POE_REC_VZ);
     return w;
+}
+
+static_assert(POE_MAX_MATERIALS == poe::MAX_PALETTE, "the public palette bound is the kernels' one");
+
+int poe_material_palette(const float *coef, int64_t ncell, float dt, uint8_t *ids, float *rows, int32_t *nmat)
+{
+    if (!coef || ncell < 1 || !ids || !rows || !nmat || !(dt > 0.0f)) return POE_EINVAL;
+    *nmat = 0;
+    std::vector<uint8_t> id;
+    std::vector<float> tab;
+    if (!poe::build_palette(coef, ncell, dt, id, tab)) return POE_OK;
+    // the kernels' row layout (poe::MT_*) to the public one (POE_C_*, then POE_M_*)
+    static const int from[POE_MROW] = {poe::MT_RHO, poe::MT_RHOF, poe::MT_RSM, poe::MT_EOK, poe::MT_LC,
+                                       poe::MT_MU,  poe::MT_AL,   poe::MT_M,   poe::MT_CO,  poe::MT_C1,
+                                       poe::MT_C2,  poe::MT_RHOF_EOK, poe::MT_RCO, poe::MT_RC1};
+    const int n = (int)(tab.size() / poe::MT_W);
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < POE_MROW; ++k) rows[(size_t)i * POE_MROW + k] = tab[(size_t)i * poe::MT_W + from[k]];
+    std::memcpy(ids, id.data(), (size_t)ncell);
+    *nmat = n;
+    return POE_OK;
 }
 
 const char *poe_status_string(int status)

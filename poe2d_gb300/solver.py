@@ -78,6 +78,21 @@ def coeffs_biot(materials, ids):
     return coef, float(vmax.value)
 
 
+def material_palette(coef, dt):
+    """The palette a Solver builds for coef (8 planes) and time step dt:
+    (ids of the cells' shape, rows of 14 floats per material: the 8
+    coefficients, co, c1, c2, rho_f eta/kappa, 1/co, 1/c1), or None when the
+    model runs on its 8 coefficient planes instead."""
+    coef = np.ascontiguousarray(coef, np.float32)
+    ncell = coef[0].size
+    ids = np.zeros(coef.shape[1:], np.uint8)
+    rows = np.zeros((L.MAX_MATERIALS, L.MROW), np.float32)
+    n = C.c_int32(0)
+    check(L.lib().poe_material_palette(_f(coef), ncell, float(dt), ids.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                       _f(rows), C.byref(n)))
+    return (ids, rows[:n.value].copy()) if n.value else None
+
+
 def check_courant(g, cp_max):
     """Raises PoeError(POE_ECFL) if the reference's Courant tests fail (cu:1197-1212)."""
     check(L.lib().poe_check_courant(C.byref(g), float(cp_max)))

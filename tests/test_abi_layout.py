@@ -32,6 +32,8 @@ CONSTANTS = ["POE_OK", "POE_EINVAL", "POE_ECFL", "POE_ENONFINITE", "POE_ETIMEOUT
              "POE_SG_SCALARS", "POE_SG_SAMPLES", "POE_SG_CHANNELS"]
 CONSTANTS += ["POE_C_RHO", "POE_C_RHOF", "POE_C_RSM", "POE_C_EOK", "POE_C_LAMBDAC", "POE_C_MU", "POE_C_ALPHA",
               "POE_C_RBM"]
+CONSTANTS += ["POE_MAX_MATERIALS", "POE_MROW", "POE_M_CO", "POE_M_C1", "POE_M_C2", "POE_M_RHOF_EOK", "POE_M_RCO",
+              "POE_M_RC1"]
 CONSTANTS += ["POE_F_" + f.upper() for f in ("vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22",
                                               "xi1", "xi2")]
 
@@ -93,6 +95,9 @@ def test_constants_match_python(header_facts):
     assert len(L.FIELDS) == c["POE_NFIELDS"]
     for i, f in enumerate(L.FIELDS):
         assert c["POE_F_" + f.upper()] == i, f
+    assert (L.MAX_MATERIALS, L.MROW) == (c["POE_MAX_MATERIALS"], c["POE_MROW"])
+    assert (L.M_CO, L.M_C1, L.M_C2, L.M_RHOF_EOK, L.M_RCO, L.M_RC1) == tuple(
+        c["POE_M_" + k] for k in ("CO", "C1", "C2", "RHOF_EOK", "RCO", "RC1"))
     # Solver.tune documents 0 rows, 1 columns, 2 tile-major
     assert (c["POE_ORDER_ROWS"], c["POE_ORDER_COLUMNS"], c["POE_ORDER_TILE_MAJOR"]) == (0, 1, 2)
     assert (S.MAP, S.MAP_CH, S.SCALARS, S.SAMPLES, S.CHANNELS) == (

@@ -110,3 +110,57 @@ def test_biot_config1_coefficients(poe):
     np.testing.assert_allclose(c, [2320.0, 1000.0, 1e4, 1e9, 9.826e9, 8e9, 0.7297, 9.689e9], rtol=2e-4)
     assert 3300.0 < vp < 3420.0
     assert np.all(coef == coef[:, :1, :1])
+
+
+def _patchy_coef(poe, rng, shape, nmat):
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    mats = [poe.biot_material(rho_f=1000.0 - 900.0 * i / max(nmat - 1, 1), k_f=2.25e9 / (1 + 10 * i),
+                              eta=1e-3 / (1 + i), **frame) for i in range(nmat)]
+    ids = rng.integers(0, nmat, shape).astype(np.uint8)
+    coef, _ = poe.coeffs_biot(mats, ids)
+    return coef
+
+
+@pytest.mark.parametrize("nmat", [1, 2, 17, 64])
+def test_material_palette_matches_reference_float_ops(poe, nmat):
+    """The palette poe_create builds: every cell's 8 coefficients come back
+    bit for bit from its row, and the derived entries are the reference's
+    per-cell float operations (cu:293-295, with the 0.50 double literal: a
+    double sum of two floats rounded to float is the float sum, 53 >= 2*24+2)
+    plus correctly rounded reciprocals."""
+    rng = np.random.default_rng(nmat)
+    dt = np.float32(5e-5)
+    coef = _patchy_coef(poe, rng, (37, 53), nmat)
+    pal = poe.material_palette(coef, dt)
+    assert pal is not None
+    ids, rows = pal
+    assert rows.shape == (len(np.unique(ids)), 14) and rows.shape[0] == len(np.unique(coef.reshape(8, -1), axis=1).T)
+    assert bits_equal(np.moveaxis(rows[ids][..., :8], -1, 0), coef)
+    f = np.float32
+    rho, rhof, rsm, eok = (rows[:, i] for i in range(4))
+    co = (rho * rsm - rhof * rhof) / dt
+    half = (rho * eok).astype(np.float64) * 0.50
+    c1 = (co.astype(np.float64) + half).astype(f)
+    c2 = (co.astype(np.float64) - half).astype(f)
+    assert bits_equal(rows[:, 8], co) and bits_equal(rows[:, 9], c1) and bits_equal(rows[:, 10], c2)
+    assert bits_equal(rows[:, 11], rhof * eok)
+    assert bits_equal(rows[:, 12], (1.0 / co.astype(np.float64)).astype(f))
+    assert bits_equal(rows[:, 13], (1.0 / c1.astype(np.float64)).astype(f))
+
+
+def test_material_palette_declines_large_and_degenerate_models(poe):
+    rng = np.random.default_rng(7)
+    dt = 5e-5
+    coef = _patchy_coef(poe, rng, (16, 16), 1)   # one material: density alone varies below
+    coef65 = coef.copy()
+    coef65[0] = (2000.0 + np.arange(256, dtype=np.float32) % 65).reshape(16, 16)   # 65 distinct densities
+    assert poe.material_palette(coef65, dt) is None
+    coef64 = coef.copy()
+    coef64[0] = (2000.0 + np.arange(256, dtype=np.float32) % 64).reshape(16, 16)
+    assert poe.material_palette(coef64, dt) is not None
+    flat = coef.copy()
+    flat[1] = 0.0
+    flat[2] = 0.0                                # rho m - rho_f^2 = 0: co = 0 exactly
+    assert poe.material_palette(flat, dt) is None
+    with pytest.raises(poe.PoeError):
+        poe.material_palette(coef, 0.0)
