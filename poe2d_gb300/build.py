@@ -46,6 +46,11 @@ def _flags():
                    "-I", os.path.join(ROOT, "include")]
 
 
+def resource_report(src):
+    """ptxas's per-kernel resource lines (registers, stack, spills) of a .cu unit, kept by the build."""
+    return os.path.join(BUILD, os.path.splitext(src)[0] + ".ptxas.txt")
+
+
 def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc()] + _flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
@@ -53,9 +58,14 @@ def _compile(src):
         cmd[cmd.index("-c")] = "-x"
         cmd.insert(cmd.index("-x") + 1, "c++")
         cmd.insert(cmd.index("c++") + 1, "-c")
+    else:
+        cmd[1:1] = ["-Xptxas", "-v"]   # reports only; code generation is unchanged
     out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s%s" % (" ".join(cmd), out.stdout, out.stderr))
+    if src.endswith(".cu"):
+        with open(resource_report(src), "w") as f:
+            f.write(out.stderr)
     return obj
 
 
@@ -70,7 +80,8 @@ def build(force=False, verbose=False):
     """Compile libpoe2d.so (and the CLI) if any source is newer than it."""
     os.makedirs(BUILD, exist_ok=True)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "poe2d.h")]
-    if force or _stale(LIB, deps):
+    reports = [resource_report(s) for s in SOURCES if s.endswith(".cu")]
+    if force or _stale(LIB, deps) or not all(os.path.exists(r) for r in reports):
         with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
             objs = list(ex.map(_compile, SOURCES))
         libdir = cuda_lib_dir()

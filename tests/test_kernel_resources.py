@@ -1,0 +1,86 @@
+"""Register and local-memory use of every kernel, from ptxas's own report
+(``-Xptxas -v``, kept by the build in ``poe2d_gb300/_build/*.ptxas.txt``).
+
+The step kernel runs 608 threads per CTA (18 compute warps + 1 producer) at
+one CTA per SM, so ptxas caps it at 96 registers; what does not fit goes to
+local memory.  The single-model variants and the batch variants the batched
+benchmarks run (palette models with K = 1, FAST or few-bit EXACT stencils)
+must not spill.  The remaining batch variants (K != 1, per-cell coefficients,
+or EXACT at a spacing whose 24 h needs more than 8 bits) spill a few dozen
+bytes per thread to L1-resident local memory; the bound below keeps that
+from growing unnoticed.  The surrogate kernels must not spill either.
+"""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# the step kernel's stencil modes, in template order
+MODES = {0: "FAST", 1: "EXACT_FEW", 2: "EXACT_ANY"}
+
+
+def _parse(text):
+    """{mangled name: (registers, stack bytes, spill store bytes, spill load bytes)}"""
+    out, cur, frame = {}, None, (0, 0, 0)
+    for ln in text.splitlines():
+        m = re.search(r"Function properties for (\S+)", ln)
+        if m:
+            cur, frame = m.group(1), (0, 0, 0)
+            continue
+        m = re.search(r"(\d+) bytes stack frame, (\d+) bytes spill stores, (\d+) bytes spill loads", ln)
+        if m and cur:
+            frame = tuple(int(v) for v in m.groups())
+            continue
+        m = re.search(r"Used (\d+) registers", ln)
+        if m and cur:
+            out[cur] = (int(m.group(1)),) + frame
+            cur = None
+    return out
+
+
+@pytest.fixture(scope="module")
+def reports():
+    from poe2d_gb300 import build as B
+    B.build()
+    got = {}
+    for src in B.SOURCES:
+        if src.endswith(".cu"):
+            with open(B.resource_report(src)) as f:
+                got[src] = _parse(f.read())
+    return got
+
+
+def _step_variants(rep):
+    out = {}
+    for name, res in rep.items():
+        m = re.search(r"k_tile_palILi(\d)ELb(\d)ELb(\d)ELb(\d)E", name)
+        if m:
+            sm, kone, multi, coef = (int(v) for v in m.groups())
+            out[(MODES[sm], bool(kone), bool(multi), bool(coef))] = res
+    return out
+
+
+def test_every_step_kernel_variant_is_built(reports):
+    v = _step_variants(reports["poe2d_tile.cu"])
+    assert len(v) == 3 * 2 * 2 * 2, sorted(v)
+    for key, (regs, _, _, _) in v.items():
+        assert regs <= 96, (key, regs)   # 608 threads at one CTA per SM
+
+
+def test_single_model_and_benchmarked_batch_variants_do_not_spill(reports):
+    v = _step_variants(reports["poe2d_tile.cu"])
+    for (mode, kone, multi, coef), (regs, stack, st, ld) in v.items():
+        benchmarked_batch = multi and kone and not coef and mode in ("FAST", "EXACT_FEW")
+        if not multi or benchmarked_batch:
+            assert st == 0 and ld == 0, ((mode, kone, multi, coef), st, ld)
+        else:
+            assert st <= 128 and ld <= 256, ((mode, kone, multi, coef), st, ld)
+
+
+def test_surrogate_kernels_do_not_spill(reports):
+    for src in ("sg_gemm.cu", "sg_ops.cu"):
+        assert reports[src], src
+        for name, (regs, stack, st, ld) in reports[src].items():
+            assert st == 0 and ld == 0, (name, st, ld)
