@@ -264,9 +264,11 @@ class Batch:
     """Several Solvers advanced together, one persistent launch per time step.
 
     Every solver must use the same stencil mode, and either all use the
-    material palette (the default for patchy models) or none does.  run(steps) takes one step count per
-    solver (or one for all); each solver's shots end exactly as after
-    solver.run(steps[i]).  The solvers must outlive the batch.
+    material palette (the default for patchy models) or none does.
+    run(steps) takes one step count per solver (or one for all); each
+    solver's shots end exactly as after solver.run(steps[i]).  The solvers
+    must stay open while the batch is used: run() and sync() refuse a batch
+    one of whose solvers has been closed.
     """
 
     def __init__(self, solvers, stream=None):
@@ -288,7 +290,14 @@ class Batch:
             m = L.lib().poe_batch_last_error(self.h)
             raise PoeError(st, m.decode() if m else "")
 
+    def _live(self):
+        if not getattr(self, "h", None):
+            raise PoeError(L.POE_ESTATE, "batch is closed")
+        if any(not s.h for s in self.solvers):
+            raise PoeError(L.POE_ESTATE, "a solver of this batch has been closed")
+
     def run(self, steps):
+        self._live()
         if np.isscalar(steps):
             steps = [int(steps)] * len(self.solvers)
         if len(steps) != len(self.solvers):
@@ -297,6 +306,7 @@ class Batch:
         self._check(L.lib().poe_batch_run(self.h, arr))
 
     def sync(self):
+        self._live()
         self._check(L.lib().poe_batch_sync(self.h))
 
     @property
