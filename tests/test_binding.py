@@ -16,11 +16,13 @@ def test_batch_refuses_closed_solvers_and_closed_batches(poe):
     b = Batch.__new__(Batch)          # the state Batch.__init__ leaves, without a device
     b.solvers = [Closed()]
     b.h = C.c_void_p(1)               # never passed to the library: the guard raises first
-    for call in (lambda: b.run(5), b.sync):
-        with pytest.raises(poe.PoeError) as e:
-            call()
-        assert e.value.status == 8 and "solver" in str(e.value)
-    b.h = None
+    try:
+        for call in (lambda: b.run(5), b.sync):
+            with pytest.raises(poe.PoeError) as e:
+                call()
+            assert e.value.status == 8 and "solver" in str(e.value)
+    finally:
+        b.h = None                    # Batch.__del__ must not destroy the fake handle
     for call in (lambda: b.run(5), b.sync):
         with pytest.raises(poe.PoeError) as e:
             call()
