@@ -285,9 +285,12 @@ void poe_destroy(poe_ctx *ctx);
  * runs one shot of one model per process, cu:1596-1736).  Every context must
  * be on the same device and use the same stencil mode, and either all use the
  * material palette (few distinct materials) or none does (per-cell
- * coefficient planes: many materials or POE_CTX_NO_PALETTE).  The contexts stay owned by
- * the caller and must outlive the batch; a context belongs to at most one
- * batch at a time.  stream: a cudaStream_t or NULL for a private stream. */
+ * coefficient planes: many materials or POE_CTX_NO_PALETTE).  The contexts
+ * stay owned by the caller.  A context belongs to at most one batch at a time
+ * (POE_ESTATE for a context of a live batch); destroy the batch before its
+ * contexts: a batch one of whose contexts was destroyed refuses
+ * poe_batch_run with POE_ESTATE.  stream: a cudaStream_t or NULL for a
+ * private stream. */
 typedef struct poe_batch poe_batch;
 int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **out);
 

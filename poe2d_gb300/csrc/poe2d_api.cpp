@@ -77,8 +77,13 @@ struct poe_ctx {
     int order = 0;              // work-list order (POE_ORDER_*)
     int graph_steps = kGraphSteps;   // steps per captured graph
     int tile_x = PAL_TX, tile_z = PAL_TZ;
+    poe_batch *batch = nullptr;   // the batch this context belongs to, if any
     std::string err;
 };
+
+namespace {
+void batch_forget(poe_batch *b, poe_ctx *ctx);   // a member context is being destroyed
+}
 
 namespace {
 
@@ -1066,6 +1071,7 @@ const char *poe_last_error(const poe_ctx *ctx) { return ctx ? ctx->err.c_str() :
 void poe_destroy(poe_ctx *ctx)
 {
     if (!ctx) return;
+    if (ctx->batch) batch_forget(ctx->batch, ctx);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     drop_graph(ctx);
     for (ShotHost &s : ctx->shots) free_shot(s);
@@ -1110,6 +1116,7 @@ struct poe_batch {
     std::vector<cudaGraphExec_t> graphs;
     cudaEvent_t done = nullptr;
     int64_t launches = 0;
+    bool orphaned = false;      // a member context was destroyed: the batch no longer runs
     std::string err;
 };
 
@@ -1128,6 +1135,13 @@ int bfail(poe_batch *b, int code, const std::string &msg)
             return bfail(b, e_ == cudaErrorMemoryAllocation ? POE_ENOMEM : POE_ECUDA,    \
                          std::string(#call) + ": " + cudaGetErrorString(e_));            \
     } while (0)
+
+void batch_forget(poe_batch *b, poe_ctx *ctx)
+{
+    b->ctxs.erase(std::remove(b->ctxs.begin(), b->ctxs.end(), ctx), b->ctxs.end());
+    b->orphaned = true;
+    ctx->batch = nullptr;
+}
 
 void drop_batch_graphs(poe_batch *b)
 {
@@ -1218,6 +1232,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
         if (ctxs[i]->exact != ctxs[0]->exact) return fail(ctxs[i], POE_EINVAL, "batch: mixed stencil modes");
         for (int j = 0; j < i; ++j)
             if (ctxs[j] == ctxs[i]) return fail(ctxs[i], POE_EINVAL, "batch: context listed twice");
+        if (ctxs[i]->batch) return fail(ctxs[i], POE_ESTATE, "batch: context already belongs to a batch");
     }
     poe_batch *b = new poe_batch;
     b->ctxs.assign(ctxs, ctxs + n);
@@ -1242,6 +1257,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
         poe_batch_destroy(b);
         return POE_ECUDA;
     }
+    for (poe_ctx *c : b->ctxs) c->batch = b;
     *out = b;
     return POE_OK;
 }
@@ -1249,6 +1265,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
 int poe_batch_run(poe_batch *b, const int64_t *nsteps)
 {
     if (!b) return POE_EINVAL;
+    if (b->orphaned) return bfail(b, POE_ESTATE, "a context of this batch was destroyed");
     if (!nsteps) return bfail(b, POE_EINVAL, "nsteps");
     const int n = (int)b->ctxs.size();
     for (int i = 0; i < n; ++i) {
@@ -1336,6 +1353,8 @@ const char *poe_batch_last_error(const poe_batch *b) { return b ? b->err.c_str()
 void poe_batch_destroy(poe_batch *b)
 {
     if (!b) return;
+    for (poe_ctx *c : b->ctxs)   // destroyed members already left the list
+        if (c->batch == b) c->batch = nullptr;
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_batch_graphs(b);
     cudaFree(b->models_dev);
