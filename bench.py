@@ -151,6 +151,48 @@ def leg_shots(P, stream, fast, nsteps=10000, nshots=64, single_shots=2):
             "shot0_bitwise_equal_to_single_run": same}
 
 
+def leg_orders(P, stream, fast, nsteps=2000, reps=3):
+    """Work-list orders of the step kernel: rows (the default) against
+    balanced (the same tiles dealt so every CTA of the persistent launch gets
+    an even share of edge tiles), on the benchmark shot and on one 1001x1001
+    shot.  One solver per order, each warmed once; the orders alternate over
+    reps runs of nsteps steps from a reset shot.  Results must be equal bit
+    for bit: only the order of independent tiles differs."""
+    from poe2d_gb300 import _lib as L
+    orders = {"rows": L.ORDER_ROWS, "balanced": L.ORDER_BALANCED}
+    g2, coef2, px2, pz2, src2, rec2, _ = workload()
+    g1, coef1, px1, pz1, srcs1, rec1 = shots_model(1)
+    out = {}
+    for label, (g, coef, px, pz, src, rec) in (
+            ("2001x2001 benchmark shot, 40-cell C-PML", (g2, coef2, px2, pz2, src2, rec2)),
+            ("one 1001x1001 shot, 30-cell C-PML", (g1, coef1, px1, pz1, srcs1[0], rec1))):
+        cells = (g.NX + 1) * (g.NZ + 1)
+        solvers = {}
+        for name, o in orders.items():
+            s = P.Solver(g, coef, px, pz, stream=stream.cuda_stream, fast=fast)
+            s.add_shot(src, rec)
+            s.tune(o, 64)
+            s.run(64)                                # graph capture, first touch
+            solvers[name] = s
+        t = {name: 0.0 for name in orders}
+        traces = {}
+        for r in range(reps):
+            for name, s in solvers.items():
+                s.reset_shot(0)
+                t[name] += timed(stream, lambda: s.run(nsteps))
+                if r == 0:
+                    traces[name] = s.traces()
+        for s in solvers.values():
+            s.close()
+        res = {name + "_gcells": cells * nsteps * reps / t[name] / 1e9 for name in orders}
+        res["balanced_vs_rows"] = t["rows"] / t["balanced"]
+        res["bitwise_equal"] = bool(np.array_equal(traces["rows"].view(np.uint32),
+                                                   traces["balanced"].view(np.uint32)))
+        out[label] = res
+    out["sample"] = "%d runs of %d steps per order, alternating, 64-step graphs" % (reps, nsteps)
+    return out
+
+
 def leg_uneven(P, stream, fast, nmodels, seed=7):
     """The uneven batch: nmodels independent patchy realisations, side
     U[256, 1536], steps 4 x side, one centre-surface shot each with 128
@@ -410,6 +452,7 @@ def main():
     ap.add_argument("--stencil", default="fast", choices=["fast", "exact"],
                     help="fast: plain FP32 stencils; exact: FP32 arithmetic rounded like the reference's FP64 lines")
     ap.add_argument("--no-parity", action="store_true", help="skip the fast-vs-exact drift check")
+    ap.add_argument("--no-orders", action="store_true", help="skip the work-list order comparison")
     ap.add_argument("--no-surrogate-train", action="store_true",
                     help="skip training and scoring the surrogate ensemble on its narrow family")
     ap.add_argument("--batched", type=int, default=64, metavar="M",
@@ -551,6 +594,13 @@ def main():
             if gate["accepted_rel_l2"]:
                 surrogate["heldout_rel_l2"] = gate["accepted_rel_l2"]["median"]
 
+    orders = None
+    if rank == 0 and not args.no_orders:
+        try:
+            orders = leg_orders(P, stream, fast)
+        except Exception as exc:                     # reported, never fatal to the bench line
+            orders = {"error": repr(exc)[:300]}
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_sample(g, coef, px, pz, src.ix, src.iz)
@@ -575,7 +625,7 @@ def main():
                          "palette_frac": alg_pal / step_s / 1e9 / hbm},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity, "batched": batched,
-            "surrogate": surrogate,
+            "surrogate": surrogate, "orders": orders,
         }
         print(json.dumps(line), flush=True)
     if pg:

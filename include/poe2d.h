@@ -250,14 +250,18 @@ int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_
 enum {
     POE_ORDER_ROWS = 0,       /* per shot, tile rows (the default) */
     POE_ORDER_COLUMNS = 1,    /* per shot, tile columns */
-    POE_ORDER_TILE_MAJOR = 2  /* the same tile of every shot side by side */
+    POE_ORDER_TILE_MAJOR = 2, /* the same tile of every shot side by side */
+    POE_ORDER_BALANCED = 3    /* rows, dealt so that every CTA of the persistent launch gets an
+                                 even share of edge tiles (C-PML strips, grid edges, the source:
+                                 about twice an interior tile's work) */
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 
 /* Time every (order, graph_steps in {16, 64}) pair on this context for
  * trial_steps steps, keep the fastest and report it; ms_out (may be NULL)
- * receives the 6 timings, order-major.  Every shot must be at step 0; the
- * shots are reset to step 0 afterwards. */
+ * receives the POE_AUTOTUNE_CANDIDATES timings, order-major.  Every shot
+ * must be at step 0; the shots are reset to step 0 afterwards. */
+enum { POE_AUTOTUNE_CANDIDATES = 8 };
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out);
 
 /* Steps completed by a shot. */

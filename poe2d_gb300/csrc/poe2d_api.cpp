@@ -20,6 +20,7 @@
 #include "../../include/poe2d.h"
 #include "poe2d_internal.h"
 #include "poe2d_palette.h"
+#include "poe2d_plan.h"
 
 using namespace poe;
 
@@ -151,6 +152,29 @@ void strips(const float *prof, int n1, int &lo, int &hi)
 }
 
 
+// SMs of a device: the number of CTAs of a persistent step launch
+int device_sms(int device)
+{
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || v < 1) v = 1;
+    return v;
+}
+
+// whether the step kernel takes its guarded (edge) path for the tile at
+// (x0, z0) of a shot: a grid edge, a C-PML strip or the source within the
+// tile and its halo; the same test as the kernel's interior flag
+bool tile_is_edge(const poe_ctx *ctx, int shot, int x0, int z0)
+{
+    const ModelDev &m = ctx->m;
+    const ShotHost &s = ctx->shots[(size_t)shot];
+    const int xa = x0 - 2, xb = x0 + PAL_TX + 1, za = z0 - 2, zb = z0 + PAL_TZ + 1;
+    const bool src_in = s.src_where != SRC_NONE && s.src.ix >= xa && s.src.ix <= xb && s.src.iz >= za &&
+                        s.src.iz <= zb;
+    const bool interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
+                          zb <= m.NZ - 2 && zb < m.zB && !src_in;
+    return !interior;
+}
+
 int sync_shots(poe_ctx *ctx)
 {
     if (!ctx->shots_dirty) return POE_OK;
@@ -211,6 +235,17 @@ int sync_shots(poe_ctx *ctx)
             for (int i = 0; i < ns; ++i)
                 for (int tz = 0; tz < ctx->ntz; ++tz)
                     for (int tx = 0; tx < ctx->ntx; ++tx) add(i, tx, tz);
+        }
+        if (ctx->order == POE_ORDER_BALANCED) {
+            // the same tiles, dealt so every CTA of the persistent launch gets
+            // an even share of edge tiles (poe2d_plan.h)
+            std::vector<uint8_t> edge(ctx->items.size());
+            for (size_t j = 0; j < ctx->items.size(); ++j)
+                edge[j] = tile_is_edge(ctx, ctx->items[j].y, ctx->items[j].z, ctx->items[j].w) ? 1 : 0;
+            const std::vector<int> perm = balanced_order(edge, device_sms(ctx->device));
+            std::vector<int4> dealt(ctx->items.size());
+            for (size_t p = 0; p < perm.size(); ++p) dealt[p] = ctx->items[(size_t)perm[p]];
+            ctx->items.swap(dealt);
         }
     }
     const int ni = (int)ctx->items.size();
@@ -986,7 +1021,7 @@ int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps)
 {
     if (!ctx) return POE_EINVAL;
-    if (order < POE_ORDER_ROWS || order > POE_ORDER_TILE_MAJOR || graph_steps < 1 || graph_steps > 4096)
+    if (order < POE_ORDER_ROWS || order > POE_ORDER_BALANCED || graph_steps < 1 || graph_steps > 4096)
         return fail(ctx, POE_EINVAL, "tuning: order or graph_steps out of range");
     if (order != ctx->order) ctx->shots_dirty = true;   // rebuilds the work list (and the graph)
     if (graph_steps != ctx->graph_steps) drop_graph(ctx);
@@ -1008,7 +1043,7 @@ int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t 
     CK(cudaEventCreate(&e1));
     int best = -1, rc = POE_OK;
     float best_ms = 0.0f;
-    for (int c = 0; c < 3 * 2 && rc == POE_OK; ++c) {
+    for (int c = 0; c < POE_AUTOTUNE_CANDIDATES && rc == POE_OK; ++c) {
         const int order = c / 2, gs = kSteps[c % 2];
         if ((rc = poe_tune(ctx, order, gs)) != POE_OK) break;
         if ((rc = poe_run(ctx, gs)) != POE_OK) break;        // capture the graph, first touch

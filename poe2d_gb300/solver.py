@@ -221,14 +221,15 @@ class Solver:
         self._check(L.lib().poe_set_field(self.h, shot, fid, _f(a)))
 
     def tune(self, order=0, graph_steps=64):
-        """Work-list order (0 rows, 1 columns, 2 tile-major across shots) and graph length."""
+        """Work-list order (0 rows, 1 columns, 2 tile-major across shots, 3 rows
+        dealt for an even share of edge tiles per CTA) and graph length."""
         self._check(L.lib().poe_tune(self.h, int(order), int(graph_steps)))
 
     def autotune(self, trial_steps=128):
-        """Time the 6 (order, graph_steps) candidates, keep the fastest; shots must be
+        """Time the 8 (order, graph_steps) candidates, keep the fastest; shots must be
         at step 0 and are reset after.  Returns (order, graph_steps, ms per candidate)."""
         o, g = C.c_int32(0), C.c_int32(0)
-        ms = np.zeros(6, np.float32)
+        ms = np.zeros(L.AUTOTUNE_CANDIDATES, np.float32)
         self._check(L.lib().poe_autotune(self.h, int(trial_steps), C.byref(o), C.byref(g), _f(ms)))
         return o.value, g.value, ms
 

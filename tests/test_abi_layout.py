@@ -28,7 +28,8 @@ STRUCTS = {
 CONSTANTS = ["POE_OK", "POE_EINVAL", "POE_ECFL", "POE_ENONFINITE", "POE_ETIMEOUT", "POE_ECUDA", "POE_ENOMEM",
              "POE_EIO", "POE_ESTATE", "POE_SRC_REF_DGAUSS_P", "POE_SRC_RICKER_FZ", "POE_REC_NONE", "POE_REC_VX",
              "POE_REC_VZ", "POE_REC_P", "POE_CTX_FAST_STENCIL", "POE_CTX_NO_PALETTE", "POE_NCOEF", "POE_NFIELDS",
-             "POE_ORDER_ROWS", "POE_ORDER_COLUMNS", "POE_ORDER_TILE_MAJOR", "POE_SG_MAP", "POE_SG_MAP_CH",
+             "POE_ORDER_ROWS", "POE_ORDER_COLUMNS", "POE_ORDER_TILE_MAJOR", "POE_ORDER_BALANCED",
+             "POE_AUTOTUNE_CANDIDATES", "POE_SG_MAP", "POE_SG_MAP_CH",
              "POE_SG_SCALARS", "POE_SG_SAMPLES", "POE_SG_CHANNELS"]
 CONSTANTS += ["POE_C_RHO", "POE_C_RHOF", "POE_C_RSM", "POE_C_EOK", "POE_C_LAMBDAC", "POE_C_MU", "POE_C_ALPHA",
               "POE_C_RBM"]
@@ -98,8 +99,10 @@ def test_constants_match_python(header_facts):
     assert (L.MAX_MATERIALS, L.MROW) == (c["POE_MAX_MATERIALS"], c["POE_MROW"])
     assert (L.M_CO, L.M_C1, L.M_C2, L.M_RHOF_EOK, L.M_RCO, L.M_RC1) == tuple(
         c["POE_M_" + k] for k in ("CO", "C1", "C2", "RHOF_EOK", "RCO", "RC1"))
-    # Solver.tune documents 0 rows, 1 columns, 2 tile-major
-    assert (c["POE_ORDER_ROWS"], c["POE_ORDER_COLUMNS"], c["POE_ORDER_TILE_MAJOR"]) == (0, 1, 2)
+    # Solver.tune documents 0 rows, 1 columns, 2 tile-major, 3 balanced
+    assert (L.ORDER_ROWS, L.ORDER_COLUMNS, L.ORDER_TILE_MAJOR, L.ORDER_BALANCED) == (
+        c["POE_ORDER_ROWS"], c["POE_ORDER_COLUMNS"], c["POE_ORDER_TILE_MAJOR"], c["POE_ORDER_BALANCED"]) == (0, 1, 2, 3)
+    assert L.AUTOTUNE_CANDIDATES == c["POE_AUTOTUNE_CANDIDATES"] == 4 * 2
     assert (S.MAP, S.MAP_CH, S.SCALARS, S.SAMPLES, S.CHANNELS) == (
         c["POE_SG_MAP"], c["POE_SG_MAP_CH"], c["POE_SG_SCALARS"], c["POE_SG_SAMPLES"], c["POE_SG_CHANNELS"])
 
