@@ -46,6 +46,14 @@ def test_reference_patterns():
         assert set(np.unique(m[2000:2240])) == {2.0, 3.0}
     # pattern 2 doubles pattern 1's lattice pitch: fewer circle cells
     assert (reference_pattern(2) == 2.0).sum() < (reference_pattern(1) == 2.0).sum()
+    # exact circle-cell counts from the loop bounds of patchy:17-22 and 55-60
+    # (r = 8: a disk sqrt(dx^2 + dy^2) <= r holds 197 cells):
+    #   pattern 1, pitch 16: centres x = 9..4985 (312), z = 9..233 (15); tangent
+    #     neighbours share one cell (15 x 311 across, 312 x 14 down); the last
+    #     row loses its bottom cell to row 241 of the 240-row layer
+    #   pattern 2, pitch 32: 156 x 8 disjoint disks, the last row clipped likewise
+    assert (reference_pattern(1) == 2.0).sum() == 312 * 15 * 197 - 15 * 311 - 312 * 14 - 312
+    assert (reference_pattern(2) == 2.0).sum() == 156 * 8 * 197 - 156
 
 
 def test_resample_keeps_endpoints_and_linearity():
