@@ -79,6 +79,31 @@ def test_bad_medium_id_and_short_file(tmp_path):
     assert r.returncode == 1 and "expected" in r.stderr
 
 
+def test_argument_and_input_errors_exit_with_a_message(tmp_path):
+    """Errors the reference would crash on or ignore are reported: a fluid table
+    that is not rows of 6 values or is missing, unknown options or missing
+    values (exit 2), a bad --order, a source outside the grid."""
+    d = str(tmp_path)
+    _write_case(d)
+    with open(os.path.join(d, "fluid.txt"), "a") as f:
+        f.write("1.0\n")                                     # 4 x 6 + 1 values
+    r = subprocess.run(_args(d, extra=["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 1 and "rows of 6 values" in r.stderr
+    args = _args(d, extra=["--dry-run"])
+    args[args.index("--fluid") + 1] = os.path.join(d, "no_such_table.txt")
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    r = subprocess.run([_cli(), "--frobnicate"], capture_output=True, text=True)
+    assert r.returncode == 2 and "unknown option" in r.stderr
+    r = subprocess.run([_cli(), "--nx"], capture_output=True, text=True)
+    assert r.returncode == 2 and "missing value" in r.stderr
+    r = subprocess.run([_cli(), "--order", "y"], capture_output=True, text=True)
+    assert r.returncode == 2
+    _write_case(d, isrc=NX + 5)                             # fresh, valid table; source off the grid
+    r = subprocess.run(_args(d, extra=["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 1 and "outside the grid" in r.stderr
+
+
 def test_courant_failure_returns_like_the_reference(tmp_path):
     d = str(tmp_path)
     _write_case(d)
