@@ -232,16 +232,54 @@ int poe_set_field(poe_ctx *ctx, int32_t shot, int32_t field, const float *host_i
 
 /* Full-state checkpoint of one shot: no reference counterpart (the
  * reference's vz/vx snapshots, cu:1653-1727, cannot restart a run).  The
- * image holds a header (grid and C-PML layout, source, receiver count, step
- * clock, checksum), every integrated field, the C-PML memory variables, the
- * pressure-source accumulator and the traces recorded so far, in host byte
- * order.  poe_checkpoint_load restores it into a shot of a context built
- * with the same grid, profiles and shot definition (POE_EINVAL otherwise,
- * POE_EIO on a checksum mismatch); running on from there gives the same
- * fields and traces, bit for bit, as the uninterrupted run. */
+ * image holds a header (poe_checkpoint_header below: grid, C-PML layout,
+ * spacings, time step, hashes of the profiles, coefficients and receiver
+ * list, source, step clock, checksum), every integrated field, the C-PML
+ * memory variables, the pressure-source accumulator and the traces recorded
+ * so far, in host byte order.  poe_checkpoint_load restores it into a shot
+ * of a context built with the same grid, spacings, time step, profiles,
+ * coefficients and shot definition (POE_EINVAL otherwise, POE_EIO on a
+ * checksum mismatch); running on from there gives the same fields and
+ * traces, bit for bit, as the uninterrupted run.  The first save or load on
+ * a context reads its coefficients back from the device once, to hash them. */
 int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes);
 int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capacity);
 int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_t size);
+
+/* The header that starts every checkpoint image (host byte order).  The
+ * payload follows it: the 9 integrated state planes of the current buffer
+ * (device layout: pitch P, R rows), the stress and the velocity C-PML memory
+ * on the x strips (3 x (NZ+1) x Wx floats each) and the z strips
+ * (3 x Hz x P each), the pressure-source accumulator padded to 4 floats and
+ * the traces recorded so far (steps x nrec floats).  poe_checkpoint_load
+ * accepts an image only into a shot whose context has the same grid, C-PML
+ * layout, spacings and time step (bit for bit), the same C-PML profiles
+ * (prof_hash), the same coefficients cell by cell (coef_hash: the 8 planes,
+ * whether the context keeps them or a material palette), the same source and
+ * the same receiver list (rec_hash). */
+enum { POE_CHECKPOINT_VERSION = 2 };
+typedef struct poe_checkpoint_header {
+    char magic[8];                  /* "POE2DCK1" */
+    uint32_t version;               /* POE_CHECKPOINT_VERSION */
+    uint32_t header_bytes;          /* sizeof(poe_checkpoint_header) */
+    int32_t NX, NZ, P, R, Wx, Hz;   /* grid and device layout (plane pitch, rows, strip widths) */
+    int64_t plane, steps;           /* floats per plane; steps done */
+    int32_t nrec, src_kind, src_ix, src_iz;   /* src_kind -1: no source */
+    float f0, amplitude;
+    double t_cut;
+    float dx, dz, dt;
+    int32_t reserved0;
+    uint64_t prof_hash, coef_hash, rec_hash;
+    int64_t payload_bytes;
+    uint64_t checksum;              /* of the payload */
+    uint64_t reserved[2];
+} poe_checkpoint_header;
+
+/* Read and check the header of a checkpoint image on the host (no device
+ * needed): POE_EINVAL when the buffer is not a version-2 image or is shorter
+ * than its header and payload, POE_EIO when the payload's checksum differs.
+ * out (may be NULL) receives the header. */
+int poe_checkpoint_info(const void *host_buf, int64_t size, poe_checkpoint_header *out);
 
 /* Tuning (no reference counterpart).  The step kernel walks a list of
  * (shot, tile) items, one CTA per SM; the order of that list decides which

@@ -61,6 +61,13 @@ int poe_sg_loss_grad(poe_sg *net, const void *maps_bf16, const float *scalars, c
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) with the current gradients. */
 int poe_sg_adam(poe_sg *net, float lr);
 
+/* The optimiser state, for inspection and training checkpoints, in the
+ * layout of get_params (each pointer may be NULL): Adam's first and second
+ * moments m and v, the bf16 weight copy the forward pass reads (widened to
+ * FP32, exactly), and the number of Adam steps taken since the parameters
+ * were last set. */
+int poe_sg_get_state(poe_sg *net, float *m, float *v, float *w16_f32, int64_t n, int32_t *step);
+
 /* loss_grad + adam. */
 int poe_sg_train_step(poe_sg *net, const void *maps_bf16, const float *scalars, const void *targets_bf16,
                       int32_t B, float lr, float *loss_out);

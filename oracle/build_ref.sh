@@ -11,10 +11,12 @@
 #   cu:840-845   PML constants        cu:908-909  PML scalars
 #   cu:985-1159  PML profile builder
 #
-# Exits 0 without building when the reference tree is absent (GPU hosts).
+# The reference tree is $POE2D_REFERENCE, or else a folder named
+# "reference" beside the repository's own folder.  Exits 0 without building
+# when the reference tree is absent (GPU hosts).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${POE2D_REFERENCE:-/root/reference}
+REF=${POE2D_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 CU="$REF/seismic_CPML_2D_poroelastic_withCUDA.cu"
 OUT="$HERE/_ref"
 if [ ! -r "$CU" ]; then

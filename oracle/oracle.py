@@ -128,6 +128,37 @@ def coeffs_from_medium(medium, cp, cs, rho_sat, table):
     return coef, bad
 
 
+def coeffs_biot(materials, ids):
+    """The 8 coefficient planes from direct Biot parameters, one material per
+    id, and the largest fast-P velocity of the high-frequency Biot dispersion
+    relation.  This parameterisation has no reference counterpart (the
+    reference derives its coefficients from cp, cs and rho, cu:682-713, with
+    K_s = K_b / (1 - phi)); it restates cu:697-708 with K_b = K_frame and K_s
+    given, in float64 from the float32 parameters, each plane rounded to
+    float32 once.  materials: dicts with rho_s phi k_s k_frame mu_frame rho_f
+    k_f eta kappa tortuosity."""
+    f32 = np.float32
+    tab = np.zeros((len(materials), 8), np.float32)
+    vmax = 0.0
+    for i, q in enumerate(materials):
+        q = {k: float(f32(v)) for k, v in q.items()}
+        phi, ks, kb, mu, kf, rf = q["phi"], q["k_s"], q["k_frame"], q["mu_frame"], q["k_f"], q["rho_f"]
+        rho = (1.0 - phi) * q["rho_s"] + phi * rf
+        m = q["tortuosity"] * rf / phi
+        eok = 0.0 if (q["eta"] == 0.0 or q["kappa"] == 0.0) else q["eta"] / q["kappa"]
+        alpha = 1.0 - kb / ks
+        M = 1.0 / (phi / kf + (alpha - phi) / ks)
+        lc = kb - 2.0 / 3.0 * mu + alpha * alpha * M
+        tab[i] = [rho, rf, m, eok, lc, mu, alpha, M]
+        H, Cc = lc + 2.0 * mu, alpha * M
+        A2, B2, C2 = rho * m - rf * rf, H * m + rho * M - 2.0 * Cc * rf, H * M - Cc * Cc
+        v2 = (B2 + np.sqrt(max(B2 * B2 - 4.0 * A2 * C2, 0.0))) / (2.0 * A2)
+        if v2 > 0.0:
+            vmax = max(vmax, float(np.sqrt(v2)))
+    ids = np.asarray(ids, np.uint8)
+    return np.ascontiguousarray(np.moveaxis(tab[ids], -1, 0)), float(f32(vmax))
+
+
 def source_table(kind, f0, dt, nsteps, amplitude=1.0, t_cut=0.4, dx=1.0, dz=1.0):
     tab = np.zeros(max(nsteps, 1), np.float32)
     n = lib().orc_source_table(kind, f0, amplitude, t_cut, dt, dx, dz, nsteps, _f(tab))

@@ -169,3 +169,33 @@ def loss_and_grads(params, maps, scalars, targets, bf16=True):
         else:
             dy = dcol
     return loss, join(grads)
+
+
+# Adam's constants as the network's optimiser holds them: float32 values,
+# with 1 - beta computed in float32 (poe_sg_adam, sg_ops.cu k_adam)
+ADAM_B1 = np.float32(0.9)
+ADAM_B2 = np.float32(0.999)
+ADAM_EPS = 1e-8
+
+
+def adam_step(w, g, m, v, t, lr, b1=ADAM_B1, b2=ADAM_B2, eps=ADAM_EPS):
+    """One Adam step (Kingma & Ba 2015, Algorithm 1) in float64: step t
+    (1-based) from parameters w, gradient g and moments m, v; returns the new
+    (w, m, v).  m_hat = m / (1 - b1^t), v_hat = v / (1 - b2^t),
+    w -= lr m_hat / (sqrt(v_hat) + eps)."""
+    w, g, m, v = (np.asarray(a, np.float64) for a in (w, g, m, v))
+    one_b1 = float(np.float32(1.0) - np.float32(b1))
+    one_b2 = float(np.float32(1.0) - np.float32(b2))
+    m = float(b1) * m + one_b1 * g
+    v = float(b2) * v + one_b2 * g * g
+    m_hat = m / (1.0 - float(b1) ** t)
+    v_hat = v / (1.0 - float(b2) ** t)
+    return w - lr * m_hat / (np.sqrt(v_hat) + eps), m, v
+
+
+def bf16_bits(x):
+    """float32 -> bfloat16 by round-to-nearest-even, returned as float32 bits
+    with the low 16 bits clear (finite inputs)."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32)

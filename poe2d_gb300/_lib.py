@@ -48,6 +48,21 @@ class BiotMaterial(C.Structure):
                                          "rho_f", "k_f", "eta", "kappa", "tortuosity")]
 
 
+class CheckpointHeader(C.Structure):
+    """poe_checkpoint_header: the first bytes of a checkpoint image."""
+    _fields_ = [("magic", C.c_char * 8), ("version", C.c_uint32), ("header_bytes", C.c_uint32),
+                ("NX", C.c_int32), ("NZ", C.c_int32), ("P", C.c_int32), ("R", C.c_int32), ("Wx", C.c_int32),
+                ("Hz", C.c_int32), ("plane", C.c_int64), ("steps", C.c_int64), ("nrec", C.c_int32),
+                ("src_kind", C.c_int32), ("src_ix", C.c_int32), ("src_iz", C.c_int32), ("f0", C.c_float),
+                ("amplitude", C.c_float), ("t_cut", C.c_double), ("dx", C.c_float), ("dz", C.c_float),
+                ("dt", C.c_float), ("reserved0", C.c_int32), ("prof_hash", C.c_uint64), ("coef_hash", C.c_uint64),
+                ("rec_hash", C.c_uint64), ("payload_bytes", C.c_int64), ("checksum", C.c_uint64),
+                ("reserved", C.c_uint64 * 2)]
+
+
+CHECKPOINT_VERSION = 2
+
+
 class PoeError(RuntimeError):
     def __init__(self, status, msg=""):
         self.status = status
@@ -87,6 +102,7 @@ SYMBOLS = {
     "poe_checkpoint_size": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "poe_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "poe_checkpoint_info": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CheckpointHeader)]),
     "poe_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "poe_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _fp]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
@@ -113,6 +129,7 @@ SYMBOLS = {
     "poe_sg_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "poe_sg_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "poe_sg_adam": (C.c_int, [C.c_void_p, C.c_float]),
+    "poe_sg_get_state": (C.c_int, [C.c_void_p, _fp, _fp, _fp, C.c_int64, C.POINTER(C.c_int32)]),
     "poe_sg_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float,
                                     C.POINTER(C.c_float)]),
     "poe_sg_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

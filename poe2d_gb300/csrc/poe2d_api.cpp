@@ -45,6 +45,7 @@ struct ShotHost {
     int64_t src_off = -1;
     int src_where = SRC_NONE;
     int64_t steps = 0;
+    uint64_t rec_hash = 0;   // of the receiver list (checkpoint identity)
 };
 
 struct poe_ctx {
@@ -79,6 +80,9 @@ struct poe_ctx {
     int graph_steps = kGraphSteps;   // steps per captured graph
     int tile_x = PAL_TX, tile_z = PAL_TZ;
     poe_batch *batch = nullptr;   // the batch this context belongs to, if any
+    uint64_t prof_hash = 0;       // of the C-PML profiles given to poe_create
+    uint64_t coef_hash = 0;       // of the 8 coefficient planes, computed on first checkpoint use
+    bool coef_hashed = false;
     std::string err;
 };
 
@@ -93,6 +97,24 @@ int fail(poe_ctx *c, int code, const std::string &msg)
     if (c) c->err = msg;
     return code;
 }
+
+// 64-bit hash of a stream of 32-bit words (checkpoint identities and payload)
+struct Hash64 {
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    void word(uint32_t w)
+    {
+        h = (h ^ w) * 0x100000001b3ull;
+        h ^= h >> 29;
+    }
+    void floats(const float *v, size_t n)
+    {
+        for (size_t i = 0; i < n; ++i) {
+            uint32_t w;
+            std::memcpy(&w, v + i, 4);
+            word(w);
+        }
+    }
+};
 
 #define CK(call)                                                                          \
     do {                                                                                  \
@@ -482,6 +504,12 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
         m.R = std::max((nz + TILE_Z - 1) / TILE_Z * TILE_Z, (nz + PAL_TZ - 1) / PAL_TZ * PAL_TZ) + 8;
     }
     m.plane = (int64_t)m.P * m.R;
+    {
+        Hash64 hp;
+        hp.floats(prof_x, (size_t)6 * nx);
+        hp.floats(prof_z, (size_t)6 * nz);
+        ctx->prof_hash = hp.h;
+    }
     m.dt = grid->dt;
     m.qx = make_div24(grid->dx);
     m.qz = make_div24(grid->dz);
@@ -677,6 +705,16 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
             return bad(e, "receivers");
     }
     s.nrec = nrec;
+    {
+        Hash64 hr;
+        hr.word((uint32_t)nrec);
+        for (int i = 0; i < nrec; ++i) {
+            hr.word((uint32_t)rec[i].ix);
+            hr.word((uint32_t)rec[i].iz);
+            hr.word((uint32_t)rec[i].comp);
+        }
+        s.rec_hash = hr.h;
+    }
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return bad(e, "add shot");
     ctx->shots.push_back(s);
     ctx->shots_dirty = true;
@@ -861,19 +899,10 @@ int poe_reset_shot(poe_ctx *ctx, int32_t shot)
 // traces recorded so far (steps x nrec).  The other buffer of each pair is
 // not needed: step n reads buffer (n-1)&1 only.
 namespace {
-struct CkHeader {
-    char magic[8];          // "POE2DCK1"
-    uint32_t version, header_bytes;
-    int32_t NX, NZ, P, R, Wx, Hz;
-    int64_t plane, steps;
-    int32_t nrec, src_kind, src_ix, src_iz;
-    float f0, amplitude;
-    double t_cut;
-    int64_t payload_bytes;
-    uint64_t checksum;      // of the payload, 8-byte words
-    uint64_t reserved;
-};
+typedef poe_checkpoint_header CkHeader;
 static_assert(sizeof(CkHeader) % 16 == 0, "header keeps the payload 16-byte aligned");
+static_assert(sizeof(CkHeader) == 160, "checkpoint header layout");
+constexpr char kCkMagic[8] = {'P', 'O', 'E', '2', 'D', 'C', 'K', '1'};
 
 uint64_t ck_sum(const unsigned char *p, size_t n)
 {
@@ -887,6 +916,43 @@ uint64_t ck_sum(const unsigned char *p, size_t n)
     }
     for (; i < n; ++i) h = (h ^ p[i]) * 0x100000001b3ull;
     return h;
+}
+
+// hash of the model's 8 coefficient planes over the grid, plane by plane,
+// rows of x: the same value whether the context keeps the planes or a
+// material palette (read back from the device once per context)
+int coef_hash(poe_ctx *ctx, uint64_t *out)
+{
+    if (!ctx->coef_hashed) {
+        const ModelDev &m = ctx->m;
+        const int nx = m.NX + 1, nz = m.NZ + 1;
+        Hash64 h;
+        if (ctx->ids) {
+            std::vector<uint8_t> ids((size_t)nx * nz);
+            std::vector<float> tab((size_t)ctx->nmat * MT_W);
+            CK(cudaMemcpy2DAsync(ids.data(), nx, ctx->ids + (size_t)ZH * m.P + XH, m.P, nx, nz,
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(tab.data(), ctx->mtab, sizeof(float) * tab.size(), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            // the table column of each coefficient plane (poe2d_palette.h)
+            static const int col[POE_NCOEF] = {MT_RHO, MT_RHOF, MT_RSM, MT_EOK, MT_LC, MT_MU, MT_AL, MT_M};
+            for (int c = 0; c < POE_NCOEF; ++c)
+                for (size_t j = 0; j < ids.size(); ++j) h.floats(&tab[(size_t)ids[j] * MT_W + col[c]], 1);
+        } else {
+            std::vector<float> plane((size_t)nx * nz);
+            for (int c = 0; c < POE_NCOEF; ++c) {
+                CK(cudaMemcpy2DAsync(plane.data(), sizeof(float) * nx, ctx->coef + c * m.plane + (int64_t)ZH * m.P + XH,
+                                     sizeof(float) * m.P, sizeof(float) * nx, nz, cudaMemcpyDeviceToHost, ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                h.floats(plane.data(), plane.size());
+            }
+        }
+        ctx->coef_hash = h.h;
+        ctx->coef_hashed = true;
+    }
+    *out = ctx->coef_hash;
+    return POE_OK;
 }
 
 struct CkParts {
@@ -907,11 +973,11 @@ CkParts ck_parts(const poe_ctx *ctx, const ShotHost &s)
 
 size_t ck_payload(const CkParts &c) { return c.f + 2 * c.x + 2 * c.z + c.acc + c.tr; }
 
-void ck_fill_header(const poe_ctx *ctx, const ShotHost &s, CkHeader &h)
+int ck_fill_header(poe_ctx *ctx, const ShotHost &s, CkHeader &h)
 {
     std::memset(&h, 0, sizeof h);
-    std::memcpy(h.magic, "POE2DCK1", 8);
-    h.version = 1;
+    std::memcpy(h.magic, kCkMagic, 8);
+    h.version = POE_CHECKPOINT_VERSION;
     h.header_bytes = sizeof(CkHeader);
     const ModelDev &m = ctx->m;
     h.NX = m.NX;
@@ -929,8 +995,32 @@ void ck_fill_header(const poe_ctx *ctx, const ShotHost &s, CkHeader &h)
     h.f0 = s.src_where == SRC_NONE ? 0.0f : s.src.f0;
     h.amplitude = s.src_where == SRC_NONE ? 0.0f : s.src.amplitude;
     h.t_cut = s.src_where == SRC_NONE ? 0.0 : s.src.t_cut;
+    h.dx = ctx->g.dx;
+    h.dz = ctx->g.dz;
+    h.dt = ctx->g.dt;
+    h.prof_hash = ctx->prof_hash;
+    h.rec_hash = s.rec_hash;
+    return coef_hash(ctx, &h.coef_hash);
 }
+
+bool same_bits(float a, float b) { return std::memcmp(&a, &b, 4) == 0; }
 }  // namespace
+
+int poe_checkpoint_info(const void *host_buf, int64_t size, poe_checkpoint_header *out)
+{
+    if (!host_buf || size < (int64_t)sizeof(CkHeader)) return POE_EINVAL;
+    CkHeader h;
+    std::memcpy(&h, host_buf, sizeof h);
+    if (std::memcmp(h.magic, kCkMagic, 8) || h.version != POE_CHECKPOINT_VERSION ||
+        h.header_bytes != sizeof(CkHeader) || h.payload_bytes < 0 ||
+        size - (int64_t)sizeof(CkHeader) < h.payload_bytes)
+        return POE_EINVAL;
+    if (ck_sum(static_cast<const unsigned char *>(host_buf) + sizeof(CkHeader), (size_t)h.payload_bytes) !=
+        h.checksum)
+        return POE_EIO;
+    if (out) *out = h;
+    return POE_OK;
+}
 
 int poe_checkpoint_size(poe_ctx *ctx, int32_t shot, int64_t *bytes)
 {
@@ -966,7 +1056,7 @@ int poe_checkpoint_save(poe_ctx *ctx, int32_t shot, void *host_buf, int64_t capa
     CK(cudaStreamSynchronize(ctx->stream));
     if ((rc = device_status(ctx)) != POE_OK) return rc;
     CkHeader h;
-    ck_fill_header(ctx, *s, h);
+    if ((rc = ck_fill_header(ctx, *s, h)) != POE_OK) return rc;
     h.payload_bytes = (int64_t)ck_payload(c);
     h.checksum = ck_sum(static_cast<unsigned char *>(host_buf) + sizeof(CkHeader), ck_payload(c));
     std::memcpy(host_buf, &h, sizeof h);
@@ -980,15 +1070,21 @@ int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_
     if (!host_buf || size < (int64_t)sizeof(CkHeader)) return fail(ctx, POE_EINVAL, "checkpoint too short");
     CkHeader h, want;
     std::memcpy(&h, host_buf, sizeof h);
-    if (std::memcmp(h.magic, "POE2DCK1", 8) || h.version != 1 || h.header_bytes != sizeof(CkHeader))
-        return fail(ctx, POE_EINVAL, "not a poe2d checkpoint (version 1)");
-    ck_fill_header(ctx, *s, want);
+    if (std::memcmp(h.magic, kCkMagic, 8) || h.version != POE_CHECKPOINT_VERSION || h.header_bytes != sizeof(CkHeader))
+        return fail(ctx, POE_EINVAL, "not a poe2d checkpoint of version " + std::to_string(POE_CHECKPOINT_VERSION));
+    int rc;
+    if ((rc = ck_fill_header(ctx, *s, want)) != POE_OK) return rc;
     if (h.NX != want.NX || h.NZ != want.NZ || h.P != want.P || h.R != want.R || h.Wx != want.Wx ||
         h.Hz != want.Hz || h.plane != want.plane)
         return fail(ctx, POE_EINVAL, "checkpoint of another grid or C-PML layout");
-    if (h.nrec != want.nrec || h.src_kind != want.src_kind || h.src_ix != want.src_ix || h.src_iz != want.src_iz ||
-        h.f0 != want.f0 || h.amplitude != want.amplitude || h.t_cut != want.t_cut)
-        return fail(ctx, POE_EINVAL, "checkpoint of another shot (source or receiver count differ)");
+    if (!same_bits(h.dx, want.dx) || !same_bits(h.dz, want.dz) || !same_bits(h.dt, want.dt))
+        return fail(ctx, POE_EINVAL, "checkpoint of another grid spacing or time step");
+    if (h.prof_hash != want.prof_hash) return fail(ctx, POE_EINVAL, "checkpoint of other C-PML profiles");
+    if (h.coef_hash != want.coef_hash) return fail(ctx, POE_EINVAL, "checkpoint of another model (coefficients)");
+    if (h.nrec != want.nrec || h.rec_hash != want.rec_hash || h.src_kind != want.src_kind ||
+        h.src_ix != want.src_ix || h.src_iz != want.src_iz || h.f0 != want.f0 || h.amplitude != want.amplitude ||
+        h.t_cut != want.t_cut)
+        return fail(ctx, POE_EINVAL, "checkpoint of another shot (source or receivers differ)");
     if (h.steps < 0) return fail(ctx, POE_EINVAL, "checkpoint step count");
     const int64_t keep = s->steps;
     s->steps = h.steps;
@@ -998,7 +1094,6 @@ int poe_checkpoint_load(poe_ctx *ctx, int32_t shot, const void *host_buf, int64_
         return fail(ctx, POE_EINVAL, "checkpoint size");
     const unsigned char *p = static_cast<const unsigned char *>(host_buf) + sizeof(CkHeader);
     if (ck_sum(p, ck_payload(c)) != h.checksum) return fail(ctx, POE_EIO, "checkpoint checksum mismatch");
-    int rc;
     if ((rc = poe_reset_shot(ctx, shot)) != POE_OK) return rc;   // both buffers and traces zero, clock 0
     if ((rc = ensure_trace(ctx, *s, h.steps)) != POE_OK) return rc;
     const int b = (int)(h.steps & 1);

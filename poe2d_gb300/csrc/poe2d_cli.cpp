@@ -17,11 +17,13 @@
 // reference prints its floats.
 //
 // The reference's hard-coded constants are the defaults; flags override
-// them.  Differences: every one of the NSTEP steps is run (the reference runs
-// NSTEP/samp*samp of them, cu:1620), errors exit non-zero with a message
-// (the reference crashed on a missing model file), and a Courant failure
-// prints the reference's message and returns 0 as the reference does
-// (cu:1200-1212).
+// them.  Differences: every one of the NSTEP steps is run, where the
+// reference runs NSTEP/samp*samp of them (cu:1620) and leaves the trace rows
+// after those zero (cu:1251-1305 clear them, cu:1737-1905 write all NSTEP
+// rows); --ref-steps runs the reference's count and writes those zero rows.
+// Errors exit non-zero with a message (the reference crashed on a missing
+// model file), and a Courant failure prints the reference's message and
+// returns 0 as the reference does (cu:1200-1212).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -49,6 +51,7 @@ struct Opts {
     std::string checkpoint, restart;       // full-state image written at each snapshot / read at start
     char order = 'x';
     bool fast = false, dry = false, snapshots = true, medium_dump = true;
+    bool ref_steps = false;                // run NSTEP/samp*samp steps, as the reference's loop does
 };
 
 // the reference's fluid table, medium IDs 0..3 (cu:565-568, 574-575)
@@ -77,6 +80,7 @@ void usage()
         "  --no-medium-dump       skip mediumrho.ctxt\n"
         "  --checkpoint F         write the shot's full state to F at every snapshot (restartable)\n"
         "  --restart F            continue from a --checkpoint image of the same run\n"
+        "  --ref-steps            run NSTEP/samp*samp steps as the reference does; later trace rows are 0\n"
         "  --dry-run              read and check inputs, build coefficients and profiles, no GPU\n";
 }
 
@@ -113,6 +117,7 @@ bool parse(int argc, char **argv, Opts &o)
         else if (a == "--dry-run") o.dry = true;
         else if (a == "--no-snapshots") o.snapshots = false;
         else if (a == "--no-medium-dump") o.medium_dump = false;
+        else if (a == "--ref-steps") o.ref_steps = true;
         else { std::cerr << "unknown option " << a << "\n"; usage(); return false; }
 #undef INT_OPT
 #undef FLT_OPT
@@ -283,8 +288,10 @@ int main(int argc, char **argv)
         return 1;
     }
     if (o.medium_dump && !write_raw(path(o.out_dir, "mediumrho.ctxt"), cp.data(), n)) return 1;
+    // steps the loop runs: all of them, or the reference's whole chunks (cu:1620)
+    const int64_t nrun = o.ref_steps ? nstep / o.samp * o.samp : nstep;
     std::cout << "grid " << nx1 << " x " << nz1 << ", NSTEP=" << nstep << ", source (" << isrc << ", " << jsrc
-              << "), f0=" << f0 << ", " << nrec << " receivers\n";
+              << "), f0=" << f0 << ", " << nrec << " receivers, " << nrun << " steps run\n";
     if (o.dry) return 0;
     medium.clear();
     cs.clear();
@@ -311,12 +318,12 @@ int main(int argc, char **argv)
         if ((st = poe_checkpoint_load(ctx, shot, img.data(), (int64_t)img.size())) != POE_OK)
             return fail(ctx, st, "restart");
         poe_steps_done(ctx, shot, &done);
-        if (done > nstep) return fail(ctx, POE_EINVAL, "checkpoint is past NSTEP");
+        if (done > nrun) return fail(ctx, POE_EINVAL, "checkpoint is past the steps to run");
     }
     std::vector<float> snap(o.snapshots ? n : 0);
     char name[128];
-    while (done < nstep) {   // chunks of samp steps with their snapshots (cu:1620-1727)
-        const int64_t k = std::min<int64_t>(o.samp - done % o.samp, nstep - done);
+    while (done < nrun) {   // chunks of samp steps with their snapshots (cu:1620-1727)
+        const int64_t k = std::min<int64_t>(o.samp - done % o.samp, nrun - done);
         if ((st = poe_run(ctx, k)) != POE_OK) return fail(ctx, st, "run");
         done += k;
         if (done % o.samp == 0 && !o.checkpoint.empty()) {
@@ -340,7 +347,8 @@ int main(int argc, char **argv)
         }
         std::printf("\nStep = %5d\n", (int)done);
     }
-    std::vector<float> tr((size_t)nstep * nrec);
+    // NSTEP rows; rows past the steps run stay 0, as the reference's cleared arrays do
+    std::vector<float> tr((size_t)nstep * nrec, 0.0f);
     if ((st = poe_get_traces(ctx, shot, tr.data(), (int64_t)tr.size())) != POE_OK) return fail(ctx, st, "traces");
     poe_destroy(ctx);
 

@@ -397,6 +397,36 @@ static int params_io(poe_sg *net, float *host, const float *in, int64_t n, float
     return 0;
 }
 
+int poe_sg_get_state(poe_sg *net, float *m, float *v, float *w16_f32, int64_t n, int32_t *step)
+{
+    if (!net) return 1;
+    cudaStreamSynchronize(net->stream);
+    int rc = 0;
+    if (m && (rc = params_io(net, m, nullptr, n, net->m32, false))) return rc;
+    if (v && (rc = params_io(net, v, nullptr, n, net->v32, false))) return rc;
+    if (w16_f32) {
+        if (n != real_count(net)) return fail(net, 1, "parameter array length");
+        // the bf16 copy widened to FP32 (exact), then the compact layout
+        std::vector<uint16_t> h16((size_t)net->nparam);
+        if (cudaMemcpy(h16.data(), net->w16, sizeof(uint16_t) * h16.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(net, 5, "parameter copy");
+        std::vector<float> wide(h16.size());
+        for (size_t i = 0; i < h16.size(); ++i) {
+            const uint32_t bits = (uint32_t)h16[i] << 16;
+            std::memcpy(&wide[i], &bits, 4);
+        }
+        float *tmp = nullptr;
+        if (cudaMalloc(&tmp, sizeof(float) * wide.size()) != cudaSuccess) return fail(net, 6, "state copy");
+        rc = cudaMemcpy(tmp, wide.data(), sizeof(float) * wide.size(), cudaMemcpyHostToDevice) == cudaSuccess
+                 ? params_io(net, w16_f32, nullptr, n, tmp, false)
+                 : fail(net, 5, "state copy");
+        cudaFree(tmp);
+        if (rc) return rc;
+    }
+    if (step) *step = net->adam_t;
+    return 0;
+}
+
 int poe_sg_get_params(poe_sg *net, float *host, int64_t n)
 {
     if (!net || !host) return 1;

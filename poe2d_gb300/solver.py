@@ -128,6 +128,18 @@ def ref_receivers(g, isource, jsource, panj, panj2, a0_pos, a1_pos):
     return np.array([(arr[i].ix, arr[i].iz, arr[i].comp) for i in range(n)], np.int32)
 
 
+def checkpoint_info(image):
+    """Header of a checkpoint image as a dict, checked on the host (no GPU):
+    PoeError(EINVAL) for a buffer that is not a version-2 image or is shorter
+    than its payload, PoeError(EIO) for a payload checksum mismatch."""
+    buf = np.frombuffer(image, np.uint8)
+    h = L.CheckpointHeader()
+    check(L.lib().poe_checkpoint_info(buf.ctypes.data_as(C.c_void_p), buf.size, C.byref(h)))
+    out = {name: getattr(h, name) for name, _ in L.CheckpointHeader._fields_ if not name.startswith("reserved")}
+    out["magic"] = bytes(h.magic)
+    return out
+
+
 def wait_limit_check(polls=1000, device=0):
     """Run the kernels' bounded mbarrier wait against a barrier nothing arrives
     at (poe_wait_limit_check): True when the wait gave up at its limit."""

@@ -82,6 +82,14 @@ class Surrogate:
                                              maps.shape[0], C.byref(loss)))
         return loss.value
 
+    def state(self):
+        """Adam state: (m, v, bf16 weight copy as FP32, steps taken), compact layout."""
+        m, v, w16 = (np.empty(self.nparam, np.float32) for _ in range(3))
+        t = C.c_int32(0)
+        self._check(L.lib().poe_sg_get_state(self.h, m.ctypes.data_as(L._fp), v.ctypes.data_as(L._fp),
+                                             w16.ctypes.data_as(L._fp), self.nparam, C.byref(t)))
+        return m, v, w16, t.value
+
     def adam(self, lr):
         self._check(L.lib().poe_sg_adam(self.h, float(lr)))
 

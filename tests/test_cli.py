@@ -113,6 +113,20 @@ def test_courant_failure_returns_like_the_reference(tmp_path):
     assert r.returncode == 0 and "time step is too large" in r.stdout
 
 
+def test_ref_steps_runs_the_references_whole_chunks(tmp_path):
+    """The reference's loop runs NSTEP/samp*samp steps (cu:1620); --ref-steps
+    does the same, without it every step runs."""
+    d = str(tmp_path)
+    _write_case(d, nstep=130)
+    r = subprocess.run(_args(d, extra=["--dry-run"]), capture_output=True, text=True)
+    assert r.returncode == 0 and "130 steps run" in r.stdout, r.stdout
+    r = subprocess.run(_args(d, extra=["--dry-run", "--ref-steps"]), capture_output=True, text=True)
+    assert r.returncode == 0 and "NSTEP=130" in r.stdout and "128 steps run" in r.stdout, r.stdout
+    _write_case(d, nstep=50)                                  # NSTEP < samp: the reference runs no step
+    r = subprocess.run(_args(d, extra=["--dry-run", "--ref-steps"]), capture_output=True, text=True)
+    assert r.returncode == 0 and " 0 steps run" in r.stdout, r.stdout
+
+
 def _fmt_rows(a):
     return "".join("".join("%g " % float(v) for v in row) + "\n" for row in a)
 
@@ -168,3 +182,31 @@ def test_cli_restart_from_checkpoint_gives_the_same_files(tmp_path):
     for name in ("recvspvz00000200.vsp", "rechorvx00000200.hor", "recsrc00000200.src"):
         assert (a / name).read_bytes() == (b / name).read_bytes(), name
     assert not (b / "vz00064.vzo").exists()          # restarted past the first snapshot
+
+
+@pytest.mark.gpu
+def test_cli_ref_steps_writes_zero_rows_past_the_last_chunk(tmp_path, poe):
+    """With --ref-steps and NSTEP % samp != 0 the files hold NSTEP rows: the
+    first NSTEP/samp*samp are the run's, the rest are 0, as the reference
+    writes its cleared trace arrays (cu:1251-1305, 1737-1905)."""
+    d = str(tmp_path)
+    nstep, isrc, jsrc, f0 = 130, 60, 50, 200.0
+    medium, cp, cs, rho = _write_case(d, "x", nstep, isrc, jsrc, f0)
+    r = subprocess.run(_args(d, "x", ["--ref-steps", "--no-snapshots"]), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    from tests.golden.make_golden import LOOP_TABLE
+    g = poe.grid(NX, NZ, 0.5, 5e-5)
+    coef = poe.coeffs_from_medium(g, medium, cp, cs, rho, LOOP_TABLE)
+    px, pz = poe.pml_profiles(g, 10, f0, float(cp.max()))
+    rec = poe.ref_receivers(g, isrc, jsrc, 10, 12, 30, 70)
+    with poe.Solver(g, coef, px, pz) as s:
+        s.add_shot(poe.source(isrc, jsrc, poe.SRC_REF_DGAUSS_P, f0, 1.0, 0.4), rec)
+        s.run(128)
+        tr = np.zeros((nstep, len(rec)), np.float32)
+        tr[:128] = s.traces()
+    assert np.abs(tr[:128]).max() > 0
+    with open(os.path.join(d, "rechorvz%08d.hor" % int(f0))) as f:
+        assert f.read() == _fmt_rows(tr[:, 20:32])
+    with open(os.path.join(d, "recsrc%08d.src" % int(f0))) as f:
+        assert f.read() == "".join("%g " % float(v) for v in tr[:, 47])
+    assert not os.path.exists(os.path.join(d, "vz%05d.vzo" % 128))

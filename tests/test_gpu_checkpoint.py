@@ -85,3 +85,55 @@ def test_checkpoint_rejects_mismatch_and_corruption(poe):
     a.restore(img, 0)
     assert a.steps(0) == 40
     a.close()
+
+
+def test_checkpoint_rejects_another_model_or_geometry(poe):
+    """The header carries the spacings, the time step and hashes of the
+    profiles, the coefficients and the receiver list: an image loads only
+    into a shot of the same model and geometry, whatever the grid layout."""
+    g, coef, px, pz, rec, srcs = m = _model(poe, True)
+    a = _open(poe, m, True)
+    a.run(30)
+    img = a.checkpoint(0)
+    info = poe.checkpoint_info(img)
+    assert info["steps"] == 30 and info["nrec"] == len(rec) and info["dt"] == np.float32(5e-5)
+    a.close()
+
+    def refused(g2, coef2, px2, pz2, rec2, palette=True):
+        s = poe.Solver(g2, coef2, px2, pz2, palette=palette)
+        s.add_shot(srcs[0], rec2)
+        with pytest.raises(poe.PoeError) as e:
+            s.restore(img, 0)
+        s.close()
+        return e.value.status
+
+    px2, pz2 = poe.pml_profiles(g, 12, 230.0, 3500.0)           # same strips, other damping
+    assert px2.shape == px.shape and not np.array_equal(px2, px)
+    assert refused(g, coef, px2, pz2, rec) == 1
+    g2 = poe.grid(g.NX, g.NZ, g.dx, 4e-5)                        # another time step, same profiles
+    assert refused(g2, coef, px, pz, rec) == 1
+    coef2 = coef.copy()
+    coef2[4, 70, 90] *= np.float32(1.0001)                       # one cell's lambda_c: a third material
+    assert refused(g, coef2, px, pz, rec) == 1
+    assert refused(g, coef2, px, pz, rec, palette=False) == 1
+    rec2 = list(rec)
+    rec2[5] = (rec2[5][0] + 1, rec2[5][1], rec2[5][2])          # one receiver moved by a cell
+    assert refused(g, coef, px, pz, rec2) == 1
+
+
+def test_checkpoint_moves_between_palette_and_planes(poe):
+    """The coefficient hash is taken over the 8 planes, so an image saved by a
+    context that keeps a material palette restores into one that keeps the
+    planes (the same model), and the run goes on bit for bit."""
+    m = _model(poe, True)
+    a = _open(poe, m, True)
+    a.run(64)
+    img = a.checkpoint(1)
+    a.run(40)
+    want = _snap(a, 1)
+    a.close()
+    b = _open(poe, m, False)
+    b.restore(img, 1)
+    b.run(40)
+    _eq(_snap(b, 1), want)
+    b.close()

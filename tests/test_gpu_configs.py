@@ -1,0 +1,139 @@
+"""GPU parity at the benchmark configurations, against the oracle.
+
+Every case runs the shot on the GPU with the reference's rounding (EXACT)
+and with plain FP32 stencils (FAST, the benchmarked path) and compares both
+with the oracle's REFMIXED loop (FP32 storage, FP64 stencil temporaries: the
+reference's own arithmetic) on the same inputs:
+
+  * sandstone 201 x 201, in full: homogeneous water-saturated sandstone,
+    h = 0.5 m, 20-cell C-PML (R = 1e-3, power 2, alpha_max = pi f0),
+    dt = 5e-5 s, 2000 steps, vertical-force Ricker f0 = 200 Hz at the grid
+    centre, 11 receivers x (vx, vz, p) on a line 20 m (40 cells) above it;
+  * the 2001 x 2001 patchy benchmark shot (40-cell C-PML, Ricker at the
+    surface centre, 400 surface receivers x 3) at full size for 300 steps;
+  * the reference's own grid, 13600 x 2440 cells (cu:486-487, h = 1.25 m,
+    dt = 95e-6 s, 10-cell C-PML, cu:493-513), with the reference's source
+    (dGauss on p, cu:90-111) and its full receiver geometry (panj = 122,
+    panj2 = 680, save1_kernel cu:114-201), layered medium, 100 steps.
+
+Bars (the stated tolerance): traces relative L2 <= 1e-5 per component and
+every snapshot field's largest error <= 1e-5 of that field's peak, for FAST;
+EXACT must equal the oracle bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+SNAP_FIELDS = ("vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22", "xi1", "xi2")
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def sandstone_201(P):
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = P.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    n = 200
+    coef, vp = P.coeffs_biot([water], np.zeros((n + 1, n + 1), np.uint8))
+    g = P.grid(n, n, 0.5, 5e-5)
+    P.check_courant(g, vp)
+    px, pz = P.pml_profiles(g, 20, 200.0, vp)
+    src = P.source(100, 100, P.SRC_RICKER_FZ, 200.0, 1e6, 0.0)
+    rec = [(x, 60, c) for c in (P.REC_VX, P.REC_VZ, P.REC_P) for x in range(50, 151, 10)]
+    return g, coef, px, pz, src, rec, 2000
+
+
+def patchy_2001(P):
+    import bench
+    g, coef, px, pz, src, rec, _ = bench.workload()
+    return g, coef, px, pz, src, rec, 300
+
+
+def reference_grid(P):
+    """13600 x 2440, the reference's constants; a layered medium of 8 layers
+    whose medium IDs alternate over the 4 fluid rows (at most 32 materials:
+    the palette kernel), cp 2600-3400 m/s."""
+    from tests.golden.make_golden import LOOP_TABLE
+    NX, NZ, dx, dt, f0 = 13599, 2439, 1.25, 95e-6, 200.0
+    nz1, nx1 = NZ + 1, NX + 1
+    layer = (np.arange(nz1) * 8) // nz1                          # 8 horizontal layers
+    cp_l = np.linspace(2600.0, 3400.0, 8).astype(np.float32)
+    cs_l = (cp_l / 1.9).astype(np.float32)
+    rho_l = np.linspace(2100.0, 2500.0, 8).astype(np.float32)
+    cp = np.repeat(cp_l[layer][:, None], nx1, axis=1)
+    cs = np.repeat(cs_l[layer][:, None], nx1, axis=1)
+    rho = np.repeat(rho_l[layer][:, None], nx1, axis=1)
+    medium = ((layer[:, None] + (np.arange(nx1)[None, :] // 1700)) % 4).astype(np.float32)
+    g = P.grid(NX, NZ, dx, dt)
+    coef = P.coeffs_from_medium(g, medium, cp, cs, rho, LOOP_TABLE)
+    P.check_courant(g, float(cp.max()))
+    px, pz = P.pml_profiles(g, 10, f0, float(cp.max()))
+    isrc, jsrc = 6800, 40
+    rec = P.ref_receivers(g, isrc, jsrc, 122, 680, 60, 120)      # cu:496-497; a0, a1 near the source row
+    src = P.source(isrc, jsrc, P.SRC_REF_DGAUSS_P, f0, 1.0, 0.4)
+    return g, coef, px, pz, src, rec, 100
+
+
+CASES = {"sandstone201_2000steps": sandstone_201, "patchy2001_300steps": patchy_2001,
+         "reference_grid_13600x2440_100steps": reference_grid}
+
+
+@pytest.fixture(scope="module")
+def oracle_runs(poe, oracle_mod):
+    """One REFMIXED oracle run per case (traces and the 12 final fields)."""
+    O = oracle_mod
+    out = {}
+
+    def get(name):
+        if name not in out:
+            g, coef, px, pz, src, rec, n = CASES[name](poe)
+            o = O.Oracle(O.REFMIXED, g.NX, g.NZ, g.dx, g.dz, g.dt, coef, px, pz)
+            where = O.SRC_FZ if src.kind == poe.SRC_RICKER_FZ else O.SRC_P
+            o.set_source(src.ix, src.iz, where, O.source_table(src.kind, src.f0, g.dt, n, amplitude=src.amplitude,
+                                                               t_cut=src.t_cut, dx=g.dx, dz=g.dz))
+            o.set_receivers(np.asarray([(r[0], r[1], r[2]) for r in rec], np.int32))
+            tr = o.run(n)
+            fields = {f: o.field(f) for f in SNAP_FIELDS}
+            del o
+            out[name] = ((g, coef, px, pz, src, rec, n), tr, fields)
+        return out[name]
+    return get
+
+
+def _gpu(poe, case, fast):
+    g, coef, px, pz, src, rec, n = case
+    with poe.Solver(g, coef, px, pz, fast=fast) as s:
+        s.add_shot(src, rec)
+        s.run(n)
+        return s.traces(), {f: s.field(f) for f in SNAP_FIELDS}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_exact_equals_oracle_bit_for_bit(poe, oracle_runs, name):
+    case, ref_tr, ref_f = oracle_runs(name)
+    tr, fields = _gpu(poe, case, fast=False)
+    assert np.abs(ref_tr).max() > 0
+    assert np.array_equal(tr.view(np.uint32), ref_tr.view(np.uint32)), rel_l2(tr, ref_tr)
+    for f in SNAP_FIELDS:
+        assert np.array_equal(fields[f].view(np.uint32), ref_f[f].view(np.uint32)), f
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fast_within_tolerance_of_oracle(poe, oracle_runs, name):
+    case, ref_tr, ref_f = oracle_runs(name)
+    tr, fields = _gpu(poe, case, fast=True)
+    rec = case[5]
+    comps = np.asarray([r[2] for r in rec])
+    for c in (poe.REC_VX, poe.REC_VZ, poe.REC_P):
+        sel = comps == c
+        if not sel.any() or not np.abs(ref_tr[:, sel]).max() > 0:
+            continue
+        assert rel_l2(tr[:, sel], ref_tr[:, sel]) <= TOL, (name, c, rel_l2(tr[:, sel], ref_tr[:, sel]))
+    for f in SNAP_FIELDS:
+        peak = float(np.abs(ref_f[f]).max())
+        assert peak > 0, f
+        err = float(np.abs(fields[f].astype(np.float64) - ref_f[f]).max())
+        assert err <= TOL * peak, (name, f, err / peak)

@@ -5,7 +5,8 @@ Bar: the default (exact-rounding) kernels reproduce the reference's
 FP32/FP64 arithmetic: against the golden run of the reference's own code
 every trace value and every field is bit-identical; against the oracle on
 other models, relative L2 <= 1e-6 and max |diff| <= 1e-6 x peak.  The
-fast-stencil variant must meet the stated tolerance, relative L2 <= 1e-5.
+fast-stencil variant must meet the stated tolerance: relative L2 <= 1e-5 on
+the traces and a largest snapshot error <= 1e-5 of the field's peak.
 """
 import os
 
@@ -90,7 +91,8 @@ def test_two_shots_vs_oracle(poe, oracle_mod, fast):
                 assert rel_l2(tr[:, sl], ref[:, sl]) <= tol, (i, c, rel_l2(tr[:, sl], ref[:, sl]))
             for name in ("vz", "p", "sxz", "wx"):
                 r = o.field(name)
-                assert max_rel_peak(s.field(name, i), r, np.abs(r).max()) <= 10 * tol, (i, name)
+                err = max_rel_peak(s.field(name, i), r, np.abs(r).max())
+                assert err <= tol, (i, name, err)
 
 
 def test_reset_reproduces_and_fields_roundtrip(poe, oracle_mod):
@@ -157,4 +159,4 @@ def test_palette_path_matches_planes_and_oracle(poe, oracle_mod, fast):
     tol = TOL_FAST if fast else TOL_EXACT
     assert rel_l2(out[True][0], ref) <= tol
     r = o.field("vz")
-    assert max_rel_peak(out[True][1], r, np.abs(r).max()) <= 10 * tol
+    assert max_rel_peak(out[True][1], r, np.abs(r).max()) <= tol

@@ -75,3 +75,41 @@ def test_params_roundtrip_and_training_fits_a_batch(poe):
     assert net.launches > 0
     net.close()
     teacher.close()
+
+
+def test_adam_steps_match_numpy_adam(poe):
+    """Three poe_sg_adam steps on gradients of three batches against numpy's
+    Adam (oracle/surrogate_ref.py: bias-corrected moments, float64), each step
+    from the GPU's own state before it.  The moments m and v and the FP32
+    weights agree within 1e-6 of the magnitudes they are summed from (the
+    kernel folds the bias corrections into its step size and epsilon; its FP32
+    rounding is far below that bound, also where a sum cancels), the bf16
+    weight copy equals the FP32 weights rounded to nearest-even bit for bit,
+    and the step counter counts."""
+    from oracle import surrogate_ref as R
+    from poe2d_gb300.surrogate import Surrogate
+    net = Surrogate(max_batch=8, seed=11)
+    w = net.params().astype(np.float64)
+    m = np.zeros_like(w)
+    v = np.zeros_like(w)
+    lr = 1e-3
+    b1, one_b1 = float(R.ADAM_B1), float(np.float32(1) - R.ADAM_B1)
+    for t in (1, 2, 3):
+        maps, sc, tgt = _batch(8, 20 + t)
+        dm, ds, dt = _dev(maps, sc, tgt)
+        net.loss_grad(dm, ds, dt)
+        g = net.grads().astype(np.float64)
+        assert np.count_nonzero(g) > 0.5 * g.size
+        net.adam(lr)
+        w1, m1, v1 = R.adam_step(w, g, m, v, t, lr)
+        gm, gv, w16, steps = net.state()
+        gw = net.params()
+        assert steps == t
+        bounds = (("m", gm, m1, b1 * np.abs(m) + one_b1 * np.abs(g)), ("v", gv, v1, np.abs(v1)),
+                  ("w", gw, w1, np.abs(w) + np.abs(w1)))
+        for name, a, b, mag in bounds:
+            err = np.abs(a.astype(np.float64) - b)
+            assert np.all(err <= 1e-6 * mag + 1e-37), (t, name, float((err / (mag + 1e-37)).max()))
+        assert np.array_equal(w16.view(np.uint32), R.bf16_bits(gw)), t
+        w, m, v = gw.astype(np.float64), gm.astype(np.float64), gv.astype(np.float64)
+    net.close()

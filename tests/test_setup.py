@@ -112,6 +112,22 @@ def test_biot_config1_coefficients(poe):
     assert np.all(coef == coef[:, :1, :1])
 
 
+def test_biot_coefficients_match_oracle(poe, oracle_mod):
+    """The oracle's restatement of the direct-Biot coefficients equals the
+    library's bit for bit (planes and the dispersion-relation velocity): the
+    CPU reference arm of the bench builds its inputs with it."""
+    frame = dict(rho_s=2650.0, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    rng = np.random.default_rng(4)
+    mats = [dict(phi=float(rng.uniform(0.1, 0.3)), rho_f=rf, k_f=kf, eta=eta, **frame)
+            for rf, kf, eta in ((1000.0, 2.25e9, 1e-3), (100.0, 0.02e9, 1e-5), (700.0, 0.7e9, 0.03),
+                                (1000.0, 2.25e9, 0.0))]
+    ids = rng.integers(0, len(mats), (33, 47)).astype(np.uint8)
+    coef, vp = poe.coeffs_biot([poe.biot_material(**m) for m in mats], ids)
+    ocoef, ovp = oracle_mod.coeffs_biot(mats, ids)
+    assert np.array_equal(coef.view(np.uint32), ocoef.view(np.uint32))
+    assert np.float32(vp) == np.float32(ovp)
+
+
 def _patchy_coef(poe, rng, shape, nmat):
     frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
     mats = [poe.biot_material(rho_f=1000.0 - 900.0 * i / max(nmat - 1, 1), k_f=2.25e9 / (1 + 10 * i),
