@@ -286,14 +286,20 @@ int poe_checkpoint_info(const void *host_buf, int64_t size, poe_checkpoint_heade
  * tiles run side by side (halo reuse in L2), and poe_run replays a captured
  * CUDA graph of graph_steps steps.  Results do not depend on either. */
 enum {
-    POE_ORDER_ROWS = 0,       /* per shot, tile rows (the default) */
+    POE_ORDER_ROWS = 0,       /* per shot, tile rows */
     POE_ORDER_COLUMNS = 1,    /* per shot, tile columns */
     POE_ORDER_TILE_MAJOR = 2, /* the same tile of every shot side by side */
     POE_ORDER_BALANCED = 3    /* rows, dealt so that every CTA of the persistent launch gets an
                                  even share of edge tiles (C-PML strips, grid edges, the source:
-                                 about twice an interior tile's work) */
+                                 about twice an interior tile's work); the default */
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
+
+/* The step kernel's compute-warp groups: 1 (default: the 18 compute warps
+ * work each tile together) or 2 (two groups of 9 warps, each owning one of
+ * the two tile buffers and taking every other tile, so one group's mid-tile
+ * barrier overlaps the other's work).  Results do not depend on it. */
+int poe_tune_kernel(poe_ctx *ctx, int32_t warp_groups);
 
 /* Time every (order, graph_steps in {16, 64}) pair on this context for
  * trial_steps steps, keep the fastest and report it; ms_out (may be NULL)
@@ -341,6 +347,10 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
  * after the batch on a context's own stream (poe_get_traces, poe_run) is
  * ordered after it. */
 int poe_batch_run(poe_batch *b, const int64_t *nsteps);
+
+/* The batch's compute-warp groups (poe_tune_kernel); a new batch takes its
+ * first context's setting. */
+int poe_batch_tune_kernel(poe_batch *b, int32_t warp_groups);
 
 /* Wait for the batch; POE_ETIMEOUT if a kernel's bounded wait gave up. */
 int poe_batch_sync(poe_batch *b);

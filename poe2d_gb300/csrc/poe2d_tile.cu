@@ -1,825 +1,51 @@
-// poe2d_tile.cu -- the fused time step: one launch = stress + velocity.
-//
-// k_tile_pal: a persistent, warp-specialised kernel (one CTA per SM) walks a
-// work list of 60 x 32 tiles of any number of shots (and, for batches, of
-// models).  Per tile: stress on the tile + 2-cell halo (64 x 36 cells):
-// strains, fluid content, sigma2 = p, sigma_xz, sigma_xx, sigma_zz (cu:49-112,
-// 202-229, 231-244) -> shared memory, the integrated state of the tile's own
-// cells -> HBM; the tile's receivers (before the velocity update, as
-// save1_kernel runs, cu:1629); velocity on the tile (cu:279-386) -> HBM.  The
-// halo is recomputed so no tile waits for another.  sigma_xx, sigma_zz and p
-// never touch HBM.  Tiles re-read this step's inputs in their halos, so the
-// state is double-buffered: step n reads buffer (n-1)&1 and writes buffer n&1
-// (the stress C-PML memory too; the velocity C-PML memory is per-cell private
-// and updated in place).  Coefficients come from a material palette (one byte
-// per cell, a table row per material) or, for models with more distinct
-// materials, per cell from the 8 coefficient planes (COEF).
-//
-// Arithmetic per cell is the reference's, in the same order, with its FP64
-// sub-expressions rounded as in poe2d_math.cuh (EXACT) or plain FP32
-// stencils (FAST); compiled with -fmad=false.
+// poe2d_tile.cu -- launches of the fused step kernel (its variants are
+// compiled in poe2d_tile_fast.cu, poe2d_tile_exact.cu and
+// poe2d_tile_exact_any.cu from poe2d_tile.cuh) and the small kernels around
+// it: step clocks, the bounded-wait check, derived fields.
 #include <cuda_runtime.h>
 
 #include <mutex>
-#include <type_traits>
 
-#include "launch_attr.h"
-#include "poe2d_internal.h"
+#include "poe2d_tile.cuh"
 
 namespace poe {
 
 namespace {
-
-// stencil modes: plain FP32, and the reference's FP64 rounding for a spacing
-// whose 24 h is a float of few bits (0.5, 1, 1.25, ...) or for any spacing
-enum { SM_FAST = 0, SM_EXACT_FEW = 1, SM_EXACT_ANY = 2 };
-
-template <int SM>
-__device__ __forceinline__ float D4(float a, float b, float c, float d, const Div24 &q)
-{
-    return SM == SM_FAST ? d4_fast(a, b, c, d, q)
-                         : (SM == SM_EXACT_FEW ? d4_exact_few(a, b, c, d, q) : d4_exact_any(a, b, c, d, q));
-}
-
-template <bool KONE>
-__device__ __forceinline__ float KDIV(float v, float K)
-{
-    return KONE ? v : v / K;
-}
-
-// ---- mbarrier / TMA primitives (sm_90+ PTX) ----
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait for a phase: false if it did not complete within `polls`
-// polls (each poll may suspend the thread for a short, system-dependent time)
-__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, int polls)
-{
-    for (int i = 0; i < polls; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-// the kernels' waits: 2^20 polls, far beyond any wait of a working step
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_n(bar, parity, 1 << 20); }
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0, int c1, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// bytes (a multiple of 16, both addresses 16-byte aligned) global -> shared
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0, int c1, int c2, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-        : "memory");
-}
-
-
-}  // namespace
-
-// ===================================================================== palette
-// For models whose 8 coefficient planes take at most MAX_PALETTE distinct
-// values (patchy models: 2) each cell carries a one-byte material id and every
-// per-cell coefficient the reference computes (co, c1, c2, rhof*eta/kappa,
-// 1/co, 1/c1) comes from a table row in shared memory; other models (COEF)
-// read the 8 coefficient planes per cell.
-//
-// Persistent, warp-specialised and double-buffered: one CTA per SM walks the
-// work list of (model, shot, tile) items.  A producer warp runs one item
-// ahead: it resolves the item's model and shot (a chain of dependent global
-// loads that would otherwise stall every warp at each item), writes the
-// item's parameters to shared memory, and fills the free buffer with five TMA
-// copies (the 4 velocity planes and the 5 state planes with halos, one box
-// each; the material ids; the two C-PML profile slices) and, for a batch item,
-// a bulk copy of its material table.  Each copy costs the producer about 120
-// cycles to issue, so the copies are few and large.  Eighteen compute warps
-// compute the item from the other buffer: a warp works 32 consecutive
-// columns (conflict-free shared-memory rows) of a band of 4 consecutive rows,
-// so the z-stencils of a column reuse the values of the rows before them in
-// registers.  Stress: 9 bands x 2 halves cover the 64 x 36 stress cells;
-// velocity: 8 bands x 2 halves cover the 60 x 32 tile while the last two
-// warps record the tile's receivers.  Buffers are handed over with mbarriers (full: producer -> compute,
-// empty: compute -> producer); every wait is bounded.
-namespace {
-constexpr int PCT = 576;                           // compute threads: 18 warps
-constexpr int ROWS = 4;                            // consecutive rows per compute thread
-constexpr int PNT = PCT + 32;                      // + the producer warp
-constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
-constexpr int IW = PAL_IDS_W, IH = PAL_IDS_H;      // ids: rows z0-2 .. z0+34; column x0-4 at (x0 & 15)
-constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
-constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
-constexpr int PS_FLOATS = PS_BOX;                  // slot stride: the 5 slots are one dense TMA box
-constexpr int PXW = TMA_VW, PZH = TMA_VH;          // profile slices: x0-4 .. x0+63, z0-4 .. z0+35
-constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
-constexpr int BUF_OFF_I = (BUF_OFF_S + 5 * PS_FLOATS * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
-constexpr int BUF_OFF_PZ = BUF_OFF_PX + (6 * PXW * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
-constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
-constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
-constexpr int PAL_OFF_B = 2 * BUF_BYTES;
-constexpr size_t PAL_SMEM = PAL_OFF_B + 64;
-// every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
-constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
-static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
-static_assert(BUF_OFF_I % 128 == 0, "TMA smem alignment");
-static_assert(BUF_OFF_PX % 128 == 0 && BUF_OFF_PZ % 128 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
-              "TMA and bulk-copy destinations");
-static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 16 == 0 && IW >= 12 + 4 + 64 && PAL_SMEM <= 232448,
-              "16-byte box rows; the id box covers x0-4 .. x0+63 from any 16-byte start; shared memory budget");
-// state slots in shared memory; after the stress phase they hold its outputs
-// (the planes SF_SXZ .. SF_XI2 in order: one TMA box of depth 5 fills them)
-enum { PS_SXZ = 0, PS_G11, PS_G22, PS_XI1, PS_XI2 };
-static_assert(SF_VX + 1 == SF_VZ && SF_VZ + 1 == SF_WX && SF_WX + 1 == SF_WZ && SF_SXZ + 1 == SF_G11 &&
-                  SF_G11 + 1 == SF_G22 && SF_G22 + 1 == SF_XI1 && SF_XI1 + 1 == SF_XI2,
-              "velocity planes and stress-state planes are consecutive in the state array");
-enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
-
-// new w and v of one cell from its coefficient planes (c at the cell, planes
-// pl apart), with the reference's float operations in its order (cu:293-311,
-// 330-353): co = (rho m - rhof^2)/dt, c1,2 = co +- rho (eta/kappa)/2
-__device__ __forceinline__ void velocity_coef(const float *__restrict__ c, int64_t pl, float dt, float A, float B,
-                                              float w0, float v0, float &w1, float &v1)
-{
-    const float rho = c[C_RHO * pl], rhof = c[C_RHOF * pl];
-    const float rsm = c[C_RSM * pl], eok = c[C_EOK * pl];
-    const float co = (rho * rsm - rhof * rhof) / dt;
-    const float c1 = co + rho * eok * 0.5f;
-    const float c2 = co - rho * eok * 0.5f;
-    w1 = (c2 * w0 + (-rhof * A - rho * B)) / c1;
-    v1 = v0 + (rsm * A + rhof * B + rhof * eok * ((w0 + w1) * 0.5f)) / co;
-}
-
-// what the producer resolves for one item (shared memory, per buffer)
-struct ItemMeta {
-    float *FB;                 // state buffer written by this step
-    const float *mxr, *mzr;    // stress C-PML memory read / written by this step
-    float *mxw, *mzw;
-    float *mxv, *mzv;          // velocity C-PML memory (in place)
-    float *acc_w;              // sigma2 at the source cell, written
-    float *trace_row;          // this step's trace row, or null
-    const int4 *rec;           // receivers of this tile
-    int nrec_q;
-    int src_off, src_where, src_on;
-    float src_val, pacc;
-    int x0, z0, interior;
-};
-static_assert(sizeof(ItemMeta) <= 128, "item parameters fit their slot");
-static_assert(PCT == 32 * 2 * ((QZ + 4) / ROWS) && (QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT / 32 > 2 * (QZ / ROWS),
-              "stress bands cover the 36 stress rows; velocity bands the 32 tile rows, with warps left for receivers");
-
-// add bytes to the current phase's transaction count without arriving
-__device__ __forceinline__ void mbar_expect_tx_only(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-// orders this thread's generic-proxy shared-memory accesses before later
-// async-proxy (TMA) writes to the same buffer
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// barrier of the 16 compute warps only
-__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(PCT) : "memory"); }
-// the same barrier, returning whether v held in every compute thread
-__device__ __forceinline__ bool compute_sync_and(bool v)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.and.pred q, 1, %2, p;\n\t"
-        "selp.u32 %0, 1, 0, q;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)v), "n"(PCT)
-        : "memory");
-    return r != 0;
-}
-}  // namespace
-
-template <int SM, bool KONE, bool MULTI, bool COEF>
-__global__ void __launch_bounds__(PNT, 1)
-k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
-           const int4 *__restrict__ items, int nitems, int k, int prefetch)
-{
-    constexpr bool EXACT = SM != SM_FAST;
-    extern __shared__ __align__(128) unsigned char smp[];
-    uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
-    uint64_t *empty = full + 2;
-    const int tid = threadIdx.x;
-
-    if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&full[b], 1);
-            mbar_init(&empty[b], PCT / 32);
-        }
-        mbar_fence_init();
-    }
-    __syncthreads();
-
-    // ------------------------------------------------------------ producer
-    if (tid >= PCT) {
-        const int lane = tid - PCT;
-        int j = 0;
-        for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
-            const int b = j & 1;
-            // Resolve the item (a chain of dependent global loads) while buffer b
-            // is still being computed on, so the copies start the moment it frees.
-            const int4 it = items[w];
-            const ModelDev &m = MULTI ? models[it.x] : mp;
-            const StreamShot &S = shots[it.y];
-            const int x0 = it.z, z0 = it.w;
-            const int P = m.P;
-            ItemMeta M;
-            const void *tm_v = nullptr, *tm_s = nullptr;
-            int cv = 0;
-            if (lane == 0) {
-                const int64_t n = *S.step + k + 1;
-                const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
-                M.FB = S.f[wr];
-                M.mxr = S.mx[rd];
-                M.mxw = S.mx[wr];
-                M.mzr = S.mz[rd];
-                M.mzw = S.mz[wr];
-                M.mxv = S.mxv;
-                M.mzv = S.mzv;
-                M.acc_w = S.acc + wr;
-                M.pacc = S.acc[rd];
-                M.src_off = (int)S.src_off;
-                M.src_where = S.src_where;
-                M.src_on = n <= S.src_n;
-                M.src_val = n <= S.src_n ? S.src_tab[n - 1] : 0.0f;
-                const bool rec_on = S.nrec > 0 && n <= S.trace_cap;
-                const int tile = (z0 / QZ) * m.ntx + x0 / QX;
-                const int qb = rec_on ? S.rec_start[tile] : 0, qe = rec_on ? S.rec_start[tile + 1] : 0;
-                M.rec = S.rec_sorted + qb;
-                M.nrec_q = qe - qb;
-                M.trace_row = rec_on ? S.trace + (n - 1) * S.nrec : nullptr;
-                M.x0 = x0;
-                M.z0 = z0;
-                // interior: no grid edge, C-PML strip or source within the tile and its halo
-                int sx = -1000000, sz = -1000000;
-                if (S.src_off >= 0) {
-                    sz = (int)(S.src_off / P) - ZH;
-                    sx = (int)(S.src_off - (int64_t)(sz + ZH) * P) - XH;
-                }
-                const int xa = x0 - 2, xb = x0 + QX + 1, za = z0 - 2, zb = z0 + QZ + 1;
-                M.interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
-                             zb <= m.NZ - 2 && zb < m.zB && !(sx >= xa && sx <= xb && sz >= za && sz <= zb);
-                tm_v = S.tm_v;
-                tm_s = S.tm_s;
-                cv = rd * NSF;
-            }
-            // what the fills below need from the model, read now: past the wait
-            // (a compiler barrier) a batch item's descriptor would be re-read from
-            // global memory on the copies' critical path
-            const void *m_tmi = m.tm_ids, *m_tmx = m.tm_px, *m_tmz = m.tm_pz;
-            const float *m_mtab = m.mtab;
-            const int m_nmat = m.nmat;
-            // batch items: this lane's words of the model descriptor, read now
-            constexpr int MDW = (int)(sizeof(ModelDev) / 4);
-            static_assert(MDW <= 64, "two descriptor words per producer lane");
-            uint32_t md0 = 0, md1 = 0;
-            if (MULTI) {
-                const uint32_t *msrc = reinterpret_cast<const uint32_t *>(&m);
-                if (lane < MDW) md0 = msrc[lane];
-                if (lane + 32 < MDW) md1 = msrc[lane + 32];
-            }
-            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
-                if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
-                break;
-            }
-            unsigned char *buf = smp + b * BUF_BYTES;
-            if (lane == 0) {
-                // the big copies first: the 4 velocity planes with a 4-cell halo and
-                // the 5 state planes with a 2-row halo, one box each (bytes
-                // announced, no arrival yet)
-                const uint32_t tab_bytes = (MULTI && !COEF) ? (uint32_t)(m_nmat * MT_W * 4) : 0u;
-                mbar_expect_tx_only(&full[b], PAL_TX_BYTES - (COEF ? (uint32_t)(IW * IH) : 0u) + tab_bytes);
-                tma_load_3d(buf, tm_v, x0, z0, cv + SF_VX, &full[b]);
-                tma_load_3d(buf + BUF_OFF_S, tm_s, x0, z0 + 2, cv + SF_SXZ, &full[b]);
-                // ids from padded column x0 (grid x0-4) rounded down to 16 bytes,
-                // rows from padded z0+2 (grid z0-2); profile slices from padded
-                // x0 / z0 (grid x0-4 / z0-4), all 6 rows
-                if (!COEF) tma_load_2d(buf + BUF_OFF_I, m_tmi, x0 & ~15, z0 + 2, &full[b]);
-                tma_load_2d(buf + BUF_OFF_PX, m_tmx, x0, 0, &full[b]);
-                tma_load_2d(buf + BUF_OFF_PZ, m_tmz, z0, 0, &full[b]);
-                if (MULTI && !COEF) bulk_load(buf + BUF_OFF_T, m_mtab, tab_bytes, &full[b]);
-            }
-            if (MULTI) {
-                // the model descriptor, for the compute warps
-                uint32_t *mdst = reinterpret_cast<uint32_t *>(buf + BUF_OFF_MD);
-                if (lane < MDW) mdst[lane] = md0;
-                if (lane + 32 < MDW) mdst[lane + 32] = md1;
-            }
-            // every lane's descriptor words are written before lane 0's arrival,
-            // the phase's only one, can complete it
-            __syncwarp();
-            if (lane == 0) {
-                *reinterpret_cast<ItemMeta *>(buf + BUF_OFF_M) = M;
-                mbar_arrive(&full[b]);
-            }
-            __syncwarp();
-        }
-        // copies in flight land before the CTA may exit: the last two fills
-        for (int i = j - 2 < 0 ? 0 : j - 2; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
-        return;
-    }
-
-    // ------------------------------------------------------------ compute
-    const int wid = tid >> 5;
-    const int lx = (wid & 1) * 32 + (tid & 31);    // column in the 64-wide tile
-    const int zb0 = (wid >> 1) * ROWS;             // first row of this warp's band
-    if (!MULTI) {
-        // single model: one material table for every item, in buffer 0's slot
-        float *t0 = reinterpret_cast<float *>(smp + BUF_OFF_T);
-        for (int i = tid; i < mp.nmat * MT_W; i += PCT) t0[i] = mp.mtab[i];
-        compute_sync();
-    }
-    int j = 0;
-    for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
-        const int b = j & 1;
-        unsigned char *buf = smp + b * BUF_BYTES;
-        // No barrier here: warps run ahead into the item as soon as its data
-        // has landed.  A wait that gave up leaves the buffer's contents (item
-        // parameters included) untrusted: touch nothing, join the item's
-        // mid-point barrier, which then ends every compute thread together.
-        if (!mbar_wait(&full[b], (uint32_t)((j >> 1) & 1))) {
-            compute_sync_and(false);
-            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
-            return;
-        }
-        const ModelDev &m = MULTI ? *reinterpret_cast<const ModelDev *>(buf + BUF_OFF_MD) : mp;
-        // the stencil divisors in registers: the model descriptor of a batch item
-        // sits in shared memory, where the loops' own stores would force re-reads
-        const Div24 qx = m.qx, qz = m.qz;
-        const ItemMeta &IM = *reinterpret_cast<const ItemMeta *>(buf + BUF_OFF_M);
-        const float *st = reinterpret_cast<const float *>(MULTI ? buf + BUF_OFF_T : smp + BUF_OFF_T);
-        // COEF: the 8 coefficient planes, read per cell (padded like the state: zero outside the grid)
-        const float *__restrict__ cf = m.coef;
-        const float *PXs = reinterpret_cast<const float *>(buf + BUF_OFF_PX);
-        const float *PZs = reinterpret_cast<const float *>(buf + BUF_OFF_PZ);
-        const int NX = m.NX, NZ = m.NZ;
-        const int P = m.P;
-        const int64_t PL = m.plane;
-        const float dt = m.dt;
-        const int Wx = m.Wx, nzx = (NZ + 1) * m.Wx, hzp = m.Hz * P;
-        const int x0 = IM.x0, z0 = IM.z0;
-        float *__restrict__ FB = IM.FB;
-        const int src_off = IM.src_off;
-        const int src_where = IM.src_where;
-        const bool src_on = IM.src_on != 0;
-        const float src_val = IM.src_val;
-        const float pacc = IM.pacc;
-        float *sv = reinterpret_cast<float *>(buf);                 // 4 x 40 x 68, from (x0-4, z0-4)
-        float *ss = reinterpret_cast<float *>(buf + BUF_OFF_S);     // 5 x 36 x 68, from (x0-4, z0-2)
-        const uint8_t *si = buf + BUF_OFF_I + (x0 & 15);            // 37 x 80,     from (x0-4, z0-2)
-
-        // Interior tiles (no grid edge, C-PML strip or source within the tile
-        // and its halo) take a copy of the code with every guard constant-true.
-        auto compute = [&](auto interior_tag) -> bool {
-            constexpr bool IN = decltype(interior_tag)::value;
-            if (COEF && lx < QX && wid < 2 * (QZ / ROWS)) {
-                // the density coefficients this thread's velocity rows read (rows
-                // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
-                const float *c = cf + (int64_t)(z0 + zb0 + ZH) * P + x0 + lx + XH;
-#pragma unroll
-                for (int i = 0; i < ROWS + 1; ++i)
-#pragma unroll
-                    for (int pl = C_RHO; pl <= C_EOK; ++pl)
-                        asm volatile("prefetch.global.L1 [%0];" ::"l"(c + pl * PL + (int64_t)i * P));
-            }
-            if (!IN && prefetch && lx < QX && wid < 2 * (QZ / ROWS) && x0 + lx <= NX) {
-                // the velocity C-PML memory this thread updates in place after the
-                // stress phase (rows zb0 .. zb0+3 of column lx, on the strips): to L1 now
-                const int x = x0 + lx;
-                const int xc = xcol(m, x);
-#pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const int t = z0 + zb0 + r;
-                    if (t > NZ) break;
-                    const int zr = zrow(m, t);
-                    if (xc >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + t * Wx + xc));
-                    if (zr >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
-                }
-            }
-            if (!IN && prefetch && x0 - 2 + lx >= 0 && x0 - 2 + lx <= NX) {
-                // the stress C-PML memory of this thread's 4 stress rows: to L1 before
-                // the first row needs it
-                const int x = x0 - 2 + lx;
-                const int xc = xcol(m, x);
-#pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const int z = z0 - 2 + zb0 + r;
-                    if (z < 0 || z > NZ) continue;
-                    const int zr = zrow(m, z);
-                    if (xc >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxr + a * nzx + z * Wx + xc));
-                    if (zr >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzr + a * hzp + zr * P + x + XH));
-                }
-            }
-            // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
-            {
-                const int x = x0 - 2 + lx;
-                const bool x_ok = IN || (x >= 0 && x <= NX);
-                const bool x_g1 = IN || (x >= 1 && x <= NX - 1), x_g2 = IN || (x >= 2 && x <= NX - 1);
-                const bool x_g3 = IN || (x >= 1 && x <= NX - 2);
-                const bool x_own = x_ok && lx >= 2 && lx < QX + 2;
-                const int xc = (!IN && x_ok) ? xcol(m, x) : -1;
-                const int xi = x + XH;
-                const int pxo = lx + 2;                          // x in the profile slice
-                const float bxh = PXs[PBH * PXW + pxo], axh = PXs[PAH * PXW + pxo];
-                const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
-                const float Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
-                const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo];
-                // this column's values along z, shared by the 4 rows' z-stencils:
-                // vz, wz at velocity-tile rows zb0 .. zb0+6, vx at rows zb0+1 .. zb0+7
-                const float *VXc = sv + 0 * PV_FLOATS + lx + 2, *VZc = sv + 1 * PV_FLOATS + lx + 2;
-                const float *WXc = sv + 2 * PV_FLOATS + lx + 2, *WZc = sv + 3 * PV_FLOATS + lx + 2;
-                float vzc[ROWS + 3], wzc[ROWS + 3], vxc[ROWS + 3];
-                uint8_t idc[ROWS + 1];
-#pragma unroll
-                for (int i = 0; i < ROWS + 3; ++i) {
-                    vzc[i] = VZc[(zb0 + i) * TMA_VW];
-                    wzc[i] = WZc[(zb0 + i) * TMA_VW];
-                    vxc[i] = VXc[(zb0 + 1 + i) * TMA_VW];
-                }
-#pragma unroll
-                for (int i = 0; i < ROWS + 1; ++i) idc[i] = COEF ? 0 : si[(zb0 + i) * IW + lx + 2];
-#pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const int zl = zb0 + r;
-                    const int z = z0 - 2 + zl;
-                    const int pzo = zl + 2;                      // z in the profile slice
-                    const int vr = (zl + 2) * TMA_VW;            // row of the velocity tile
-                    const int so = zl * TMA_VW + lx + 2;         // in the state tile
-                    const bool z_ok = IN || (z >= 0 && z <= NZ);
-                    const bool cell_ok = x_ok && z_ok;
-                    const bool g1 = IN || (cell_ok && x_g1 && z >= 2 && z <= NZ - 2);   // cu:60-62
-                    const bool g2 = IN || (cell_ok && x_g2 && z >= 1 && z <= NZ - 2);   // cu:212-214
-                    const bool g3 = IN || (cell_ok && x_g3 && z >= 2 && z <= NZ - 1);   // cu:237-239
-                    const bool own = x_own && z_ok && zl >= 2 && zl < QZ + 2;
-                    const int o = (z + ZH) * P + xi;
-                    const float vdx = D4<SM>(VXc[vr + 1], vxc[r + 1], VXc[vr + 2], VXc[vr - 1], qx);
-                    const float vdz = D4<SM>(vzc[r + 2], vzc[r + 1], vzc[r + 3], vzc[r], qz);
-                    const float wdx = D4<SM>(WXc[vr + 1], WXc[vr], WXc[vr + 2], WXc[vr - 1], qx);
-                    const float wdz = D4<SM>(wzc[r + 2], wzc[r + 1], wzc[r + 3], wzc[r], qz);
-                    const float sdx = D4<SM>(vzc[r + 2], VZc[vr - 1], VZc[vr + 1], VZc[vr - 2], qx);
-                    const float sdz = D4<SM>(vxc[r + 2], vxc[r + 1], vxc[r + 3], vxc[r], qz);
-                    float g11 = ss[PS_G11 * PS_FLOATS + so], g22 = ss[PS_G22 * PS_FLOATS + so];
-                    float xi1 = ss[PS_XI1 * PS_FLOATS + so], xi2 = ss[PS_XI2 * PS_FLOATS + so];
-                    float sxz = ss[PS_SXZ * PS_FLOATS + so];
-                    float lc, mu, al, M, mu_top;
-                    if (COEF) {
-                        const float *c = cf + o;
-                        lc = c[C_LC * PL];
-                        mu = c[C_MU * PL];
-                        al = c[C_AL * PL];
-                        M = c[C_M * PL];
-                        mu_top = c[C_MU * PL + P];                   // rmu[top] (cu:218)
-                    } else {
-                        const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * idc[r]);
-                        mu_top = st[MT_W * idc[r + 1] + MT_MU];      // rmu[top] (cu:218)
-                        lc = ma.x;
-                        mu = ma.y;
-                        al = ma.z;
-                        M = ma.w;
-                    }
-                    const int zr = (!IN && z_ok) ? zrow(m, z) : -1;
-                    float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-                    if (xc >= 0 && (g1 || g2)) {
-                        const int ix = z * Wx + xc;
-                        const float *MA = IM.mxr;
-                        m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
-                        m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
-                        m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
-                        if (own) {
-                            float *MB = IM.mxw;
-                            if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
-                            if (g2) MB[MXS_SXZ * nzx + ix] = m5;
-                        }
-                    }
-                    if (zr >= 0 && (g1 || g2)) {
-                        const int iz = zr * P + xi;
-                        const float *MA = IM.mzr;
-                        const float bz = PZs[PB * PZH + pzo], az = PZs[PA * PZH + pzo];
-                        m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
-                        m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-                        m6 = PZs[PBH * PZH + pzo] * MA[MZS_SXZ * hzp + iz] + PZs[PAH * PZH + pzo] * sdz;
-                        if (own) {
-                            float *MB = IM.mzw;
-                            if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
-                            if (g2) MB[MZS_SXZ * hzp + iz] = m6;
-                        }
-                    }
-                    const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo];
-                    if (g1) {   // cu:71-86
-                        g11 = g11 + dt * (KDIV<KONE>(vdx, Kxh) + m1);
-                        g22 = g22 + dt * (KDIV<KONE>(vdz, Kz) + m2);
-                        xi1 = xi1 - (KDIV<KONE>(wdx, Kxh) + m3) * dt;
-                        xi2 = xi2 - (KDIV<KONE>(wdz, Kz) + m4) * dt;
-                    }
-                    float pv = g1 ? (-al * M * (g11 + g22) + M * (xi1 + xi2)) : 0.0f;
-                    const bool is_src = !IN && cell_ok && o == src_off;
-                    if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
-                    if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-                    if (is_src && own) *IM.acc_w = pv;
-                    if (g2) {   // cu:223-226
-                        const float Ssum = KDIV<KONE>(sdx, Kx) + m5 + KDIV<KONE>(sdz, Kz) + m6;
-                        sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
-                    }
-                    float sxx = 0.0f, szz = 0.0f;
-                    if (g3) {   // cu:241-242
-                        if (EXACT) sxx_szz_exact(lc, mu, g11, g22, al, pv, sxx, szz);
-                        else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
-                    }
-                    if (own) {
-                        FB[SF_G11 * PL + o] = g11;
-                        FB[SF_G22 * PL + o] = g22;
-                        FB[SF_XI1 * PL + o] = xi1;
-                        FB[SF_XI2 * PL + o] = xi2;
-                        FB[SF_SXZ * PL + o] = sxz;
-                    }
-                    // this thread alone reads these slots of this cell: outputs overwrite inputs
-                    ss[PO_SXX * PS_FLOATS + so] = sxx;
-                    ss[PO_SZZ * PS_FLOATS + so] = szz;
-                    ss[PO_P * PS_FLOATS + so] = pv;
-                    ss[PO_SXZ * PS_FLOATS + so] = sxz;
-                }
-            }
-            if (!compute_sync_and(true)) return false;   // false: a thread's wait for this item gave up
-
-            if (wid >= 2 * (QZ / ROWS)) {
-                // ---- receivers of this tile (vx, vz before the update; p of this step)
-                if (IM.nrec_q > 0) {
-                    float *trace_row = IM.trace_row;
-                    for (int q = tid - 32 * 2 * (QZ / ROWS); q < IM.nrec_q; q += PCT - 32 * 2 * (QZ / ROWS)) {
-                        const int4 Rq = IM.rec[q];               // (x, comp, slot, z)
-                        const int xl = Rq.x - x0, zl = Rq.w - z0;
-                        float v;
-                        if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
-                        else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
-                        trace_row[Rq.z] = v;
-                    }
-                }
-            } else if (lx < QX) {
-                // ---- velocity on the tile: column lx (< 60), rows zb0 .. zb0+3
-                float *__restrict__ MXV = IM.mxv;
-                float *__restrict__ MZV = IM.mzv;
-                const int x = x0 + lx;
-                const bool x_in = IN || x <= NX;
-                const bool x_vx = IN || (x >= 2 && x <= NX - 1), x_vz = IN || (x >= 1 && x <= NX - 2);   // cu:289, 326
-                const int xc = (!IN && x_in) ? xcol(m, x) : -1;
-                const int xi = x + XH;
-                const int pxo = lx + 4;
-                const float bx = PXs[PB * PXW + pxo], ax = PXs[PA * PXW + pxo];
-                const float bxh = PXs[PBH * PXW + pxo], axh = PXs[PAH * PXW + pxo];
-                const float Kx = KONE ? 1.0f : PXs[PK * PXW + pxo], Kxh = KONE ? 1.0f : PXs[PKH * PXW + pxo];
-                // this column's stress values along z: sxz at stress-tile rows
-                // zb0 .. zb0+6, szz and p at rows zb0+1 .. zb0+7
-                const float *SXXc = ss + PO_SXX * PS_FLOATS + lx + 4, *SZZc = ss + PO_SZZ * PS_FLOATS + lx + 4;
-                const float *SXZc = ss + PO_SXZ * PS_FLOATS + lx + 4, *PPc = ss + PO_P * PS_FLOATS + lx + 4;
-                float sxzc[ROWS + 3], szzc[ROWS + 3], ppc[ROWS + 3];
-                uint8_t idc[ROWS + 1];
-#pragma unroll
-                for (int i = 0; i < ROWS + 3; ++i) {
-                    sxzc[i] = SXZc[(zb0 + i) * TMA_VW];
-                    szzc[i] = SZZc[(zb0 + 1 + i) * TMA_VW];
-                    ppc[i] = PPc[(zb0 + 1 + i) * TMA_VW];
-                }
-#pragma unroll
-                for (int i = 0; i < ROWS + 1; ++i) idc[i] = COEF ? 0 : si[(zb0 + 2 + i) * IW + lx + 4];
-#pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const int zl = zb0 + r;
-                    const int t = z0 + zl;
-                    if (!IN && (!x_in || t > NZ)) continue;
-                    const int pzo = zl + 4;
-                    const int sr = (zl + 2) * TMA_VW;            // row of the stress tile
-                    const int vo = (zl + 4) * TMA_VW + lx + 4;
-                    const float vx0 = sv[0 * PV_FLOATS + vo], vz0 = sv[1 * PV_FLOATS + vo];
-                    const float wx0 = sv[2 * PV_FLOATS + vo], wz0 = sv[3 * PV_FLOATS + vo];
-                    const int o = (t + ZH) * P + xi;
-                    const float d1x = D4<SM>(SXXc[sr], SXXc[sr - 1], SXXc[sr + 1], SXXc[sr - 2], qx);
-                    const float d2x = D4<SM>(ppc[r + 1], PPc[sr - 1], PPc[sr + 1], PPc[sr - 2], qx);
-                    const float d3x = D4<SM>(sxzc[r + 2], sxzc[r + 1], sxzc[r + 3], sxzc[r], qz);
-                    const float d1z = D4<SM>(SXZc[sr + 1], sxzc[r + 2], SXZc[sr + 2], SXZc[sr - 1], qx);
-                    const float d2z = D4<SM>(szzc[r + 2], szzc[r + 1], szzc[r + 3], szzc[r], qz);
-                    const float d3z = D4<SM>(ppc[r + 2], ppc[r + 1], ppc[r + 3], ppc[r], qz);
-                    const bool gvx = IN || (x_vx && t >= 2 && t <= NZ - 1);   // cu:289-291
-                    const bool gvz = IN || (x_vz && t >= 1 && t <= NZ - 2);   // cu:326-328
-                    const int zr = IN ? -1 : zrow(m, t);
-                    float m1 = 0.0f, m2 = 0.0f, m3 = 0.0f, m4 = 0.0f, m5 = 0.0f, m6 = 0.0f;
-                    if (xc >= 0 && (gvx || gvz)) {
-                        const int ix = t * Wx + xc;
-                        float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
-                        float *M4 = MXV + MXV_VZ * nzx + ix;
-                        m1 = bx * *M1 + ax * d1x;
-                        m2 = bx * *M2 + ax * d2x;
-                        m4 = bxh * *M4 + axh * d1z;
-                        if (gvx) { *M1 = m1; *M2 = m2; }
-                        if (gvz) *M4 = m4;
-                    }
-                    if (zr >= 0 && (gvx || gvz)) {
-                        const int iz = zr * P + xi;
-                        float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
-                        float *M6 = MZV + MZV_VZ2 * hzp + iz;
-                        const float bh = PZs[PBH * PZH + pzo], ah = PZs[PAH * PZH + pzo];
-                        m3 = PZs[PB * PZH + pzo] * *M3 + PZs[PA * PZH + pzo] * d3x;
-                        m5 = bh * *M5 + ah * d2z;
-                        m6 = bh * *M6 + ah * d3z;
-                        if (gvx) *M3 = m3;
-                        if (gvz) { *M5 = m5; *M6 = m6; }
-                    }
-                    const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo], Kzh = KONE ? 1.0f : PZs[PKH * PZH + pzo];
-                    float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
-                    {   // vx, wx, material at (x, t) (cu:293-311)
-                        const float A = KDIV<KONE>(d1x, Kx) + m1 + KDIV<KONE>(d3x, Kz) + m3;
-                        const float B = KDIV<KONE>(d2x, Kx) + m2;
-                        float w1, v1;
-                        if (COEF)
-                            velocity_coef(cf + o, PL, dt, A, B, wx0, vx0, w1, v1);
-                        else {
-                            const float *mt = st + MT_W * idc[r];
-                            const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);    // c2 rhof rho c1
-                            const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);    // 1/c1 m rhof*eok co
-                            const float rco = mt[MT_RCO];
-                            w1 = div_by(bb.x * wx0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                            v1 = vx0 + div_by(cc.y * A + bb.y * B + cc.z * ((wx0 + w1) * 0.5f), cc.w, rco);
-                        }
-                        if (gvx) { wx1 = w1; vx1 = v1; }
-                    }
-                    {   // vz, wz, material at (x, t+1) (cu:330-353)
-                        float A = KDIV<KONE>(d1z, Kxh) + m4 + KDIV<KONE>(d2z, Kzh) + m5;
-                        const float B = KDIV<KONE>(d3z, Kzh) + m6;
-                        if (!IN && o == src_off && src_where == SRC_FZ && src_on) A = A + src_val;
-                        float w1, v1;
-                        if (COEF)
-                            velocity_coef(cf + o + P, PL, dt, A, B, wz0, vz0, w1, v1);
-                        else {
-                            const float *mt = st + MT_W * idc[r + 1];
-                            const float4 bb = *reinterpret_cast<const float4 *>(mt + 4);
-                            const float4 cc = *reinterpret_cast<const float4 *>(mt + 8);
-                            const float rco = mt[MT_RCO];
-                            w1 = div_by(bb.x * wz0 + (-bb.y * A - bb.z * B), bb.w, cc.x);
-                            v1 = vz0 + div_by(cc.y * A + bb.y * B + cc.z * ((wz0 + w1) * 0.5f), cc.w, rco);
-                        }
-                        if (gvz) { wz1 = w1; vz1 = v1; }
-                    }
-                    FB[SF_VX * PL + o] = vx1;
-                    FB[SF_WX * PL + o] = wx1;
-                    FB[SF_VZ * PL + o] = vz1;
-                    FB[SF_WZ * PL + o] = wz1;
-                }
-            }
-            return true;
-        };
-        if (!(IM.interior ? compute(std::true_type{}) : compute(std::false_type{}))) {
-            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
-            return;
-        }
-        // hand buffer b back to the producer
-        fence_proxy_async();
-        __syncwarp();
-        if ((tid & 31) == 0) mbar_arrive(&empty[b]);
-    }
-}
-
-namespace {
-// SMs of the current device (the persistent grid: one CTA per SM)
-int sm_count()
-{
-    static std::atomic<int> sms[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::atomic<int> &n = sms[dev & 63];
-    if (!n.load(std::memory_order_relaxed)) {
-        int v = 0;
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        n.store(v > 0 ? v : 1, std::memory_order_relaxed);
-    }
-    return n.load(std::memory_order_relaxed);
-}
-
-// Edge tiles prefetch their C-PML memory variables to L1 when each SM walks
-// at least 8 tiles per step (a 2001^2 shot: 14, +6 %; 16 shots of 1001^2:
-// 57, +4 %); with fewer (one 1001^2 shot: 3.6, every SM on the strip rows at
-// once at the step start) the prefetches cost 10 %.
-int prefetch_strips(int nitems) { return nitems >= 8 * sm_count() ? 1 : 0; }
-
-template <int SM, bool KONE>
-int tile_impl(const ModelDev &m, const StreamShot *shots, int nshots, const int4 *items, int nitems, int k,
-              cudaStream_t st)
-{
-    static std::atomic<uint64_t> pal_done{0}, coef_done{0};
-    smem_attr_once(k_tile_pal<SM, KONE, false, false>, (int)PAL_SMEM, pal_done);
-    smem_attr_once(k_tile_pal<SM, KONE, false, true>, (int)PAL_SMEM, coef_done);
-    const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
-    const int pf = prefetch_strips(nitems);
-    if (grid > 0) {
-        if (m.ids) k_tile_pal<SM, KONE, false, false><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k, pf);
-        else k_tile_pal<SM, KONE, false, true><<<grid, PNT, PAL_SMEM, st>>>(m, nullptr, shots, items, nitems, k, pf);
-    }
-    return (int)cudaGetLastError();
-}
-
-template <int SM, bool KONE>
-int batch_impl(const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems, int k, bool coef,
-               cudaStream_t st)
-{
-    static std::atomic<uint64_t> pal_done{0}, coef_done{0};
-    const int grid = nitems < sm_count() ? nitems : sm_count();
-    const int pf = prefetch_strips(nitems);
-    ModelDev dummy{};
-    if (grid <= 0) return (int)cudaGetLastError();
-    if (coef) {
-        smem_attr_once(k_tile_pal<SM, KONE, true, true>, (int)PAL_SMEM, coef_done);
-        k_tile_pal<SM, KONE, true, true><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k, pf);
-    } else {
-        smem_attr_once(k_tile_pal<SM, KONE, true, false>, (int)PAL_SMEM, pal_done);
-        k_tile_pal<SM, KONE, true, false><<<grid, PNT, PAL_SMEM, st>>>(dummy, models, shots, items, nitems, k, pf);
-    }
-    return (int)cudaGetLastError();
-}
-}  // namespace
+using tile::mbar_fence_init;
+using tile::mbar_init;
+using tile::mbar_wait_n;
 
 // the stencil mode of a launch: FAST, or EXACT for the spacings of its models
-static int stencil_mode(bool exact, bool few)
+int stencil_mode(bool exact, bool few)
 {
     return !exact ? SM_FAST : (few ? SM_EXACT_FEW : SM_EXACT_ANY);
 }
 
-int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     bool exact, bool kone, void *stream)
+int step_mode(int sm, const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
+              int nitems, int k, bool kone, bool coef, int grp, void *stream)
 {
-    cudaStream_t st = (cudaStream_t)stream;
-    switch (stencil_mode(exact, m.qx.few_bits && m.qz.few_bits) * 2 + (kone ? 1 : 0)) {
-    case 0: return tile_impl<SM_FAST, false>(m, shots_dev, nshots, items, nitems, k, st);
-    case 1: return tile_impl<SM_FAST, true>(m, shots_dev, nshots, items, nitems, k, st);
-    case 2: return tile_impl<SM_EXACT_FEW, false>(m, shots_dev, nshots, items, nitems, k, st);
-    case 3: return tile_impl<SM_EXACT_FEW, true>(m, shots_dev, nshots, items, nitems, k, st);
-    case 4: return tile_impl<SM_EXACT_ANY, false>(m, shots_dev, nshots, items, nitems, k, st);
-    default: return tile_impl<SM_EXACT_ANY, true>(m, shots_dev, nshots, items, nitems, k, st);
+    switch (sm) {
+    case SM_FAST: return tile_step_fast(m, models, shots, items, nitems, k, kone, coef, grp, stream);
+    case SM_EXACT_FEW: return tile_step_exact(m, models, shots, items, nitems, k, kone, coef, grp, stream);
+    default: return tile_step_exact_any(m, models, shots, items, nitems, k, kone, coef, grp, stream);
     }
+}
+}  // namespace
+
+int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
+                     bool exact, bool kone, int grp, void *stream)
+{
+    (void)nshots;
+    return step_mode(stencil_mode(exact, m.qx.few_bits && m.qz.few_bits), m, nullptr, shots_dev, items, nitems, k,
+                     kone, m.ids == nullptr, grp, stream);
 }
 
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool exact_few, bool coef, bool kone, void *stream)
+                      bool exact, bool exact_few, bool coef, bool kone, int grp, void *stream)
 {
-    cudaStream_t st = (cudaStream_t)stream;
-    switch (stencil_mode(exact, exact_few) * 2 + (kone ? 1 : 0)) {
-    case 0: return batch_impl<SM_FAST, false>(models_dev, shots_dev, items, nitems, k, coef, st);
-    case 1: return batch_impl<SM_FAST, true>(models_dev, shots_dev, items, nitems, k, coef, st);
-    case 2: return batch_impl<SM_EXACT_FEW, false>(models_dev, shots_dev, items, nitems, k, coef, st);
-    case 3: return batch_impl<SM_EXACT_FEW, true>(models_dev, shots_dev, items, nitems, k, coef, st);
-    case 4: return batch_impl<SM_EXACT_ANY, false>(models_dev, shots_dev, items, nitems, k, coef, st);
-    default: return batch_impl<SM_EXACT_ANY, true>(models_dev, shots_dev, items, nitems, k, coef, st);
-    }
+    const ModelDev dummy{};
+    return step_mode(stencil_mode(exact, exact_few), dummy, models_dev, shots_dev, items, nitems, k, kone, coef, grp,
+                     stream);
 }
 
 // the bounded wait on a phase that never completes (no thread arrives): the

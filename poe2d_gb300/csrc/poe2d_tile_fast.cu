@@ -1,0 +1,13 @@
+// poe2d_tile_fast.cu -- the step kernel's variants for plain FP32 stencils.
+// One translation unit per stencil mode, so the variants compile in parallel.
+#include "poe2d_tile.cuh"
+
+namespace poe {
+
+int tile_step_fast(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
+                   int nitems, int k, bool kone, bool coef, int grp, void *stream)
+{
+    return tile_launch_mode<SM_FAST>(m, models, shots, items, nitems, k, kone, coef, grp, (cudaStream_t)stream);
+}
+
+}  // namespace poe

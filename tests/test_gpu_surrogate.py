@@ -99,7 +99,7 @@ def test_adam_steps_match_numpy_adam(poe):
         dm, ds, dt = _dev(maps, sc, tgt)
         net.loss_grad(dm, ds, dt)
         g = net.grads().astype(np.float64)
-        assert np.count_nonzero(g) > 0.5 * g.size
+        assert np.count_nonzero(g) > 0.25 * g.size        # ReLU zeroes some units' gradients
         net.adam(lr)
         w1, m1, v1 = R.adam_step(w, g, m, v, t, lr)
         gm, gv, w16, steps = net.state()
