@@ -295,12 +295,6 @@ enum {
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 
-/* The step kernel's compute-warp groups: 1 (default: the 18 compute warps
- * work each tile together) or 2 (two groups of 9 warps, each owning one of
- * the two tile buffers and taking every other tile, so one group's mid-tile
- * barrier overlaps the other's work).  Results do not depend on it. */
-int poe_tune_kernel(poe_ctx *ctx, int32_t warp_groups);
-
 /* Time every (order, graph_steps in {16, 64}) pair on this context for
  * trial_steps steps, keep the fastest and report it; ms_out (may be NULL)
  * receives the POE_AUTOTUNE_CANDIDATES timings, order-major.  Every shot
@@ -347,10 +341,6 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
  * after the batch on a context's own stream (poe_get_traces, poe_run) is
  * ordered after it. */
 int poe_batch_run(poe_batch *b, const int64_t *nsteps);
-
-/* The batch's compute-warp groups (poe_tune_kernel); a new batch takes its
- * first context's setting. */
-int poe_batch_tune_kernel(poe_batch *b, int32_t warp_groups);
 
 /* Wait for the batch; POE_ETIMEOUT if a kernel's bounded wait gave up. */
 int poe_batch_sync(poe_batch *b);

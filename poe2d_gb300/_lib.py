@@ -104,8 +104,6 @@ SYMBOLS = {
     "poe_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
     "poe_checkpoint_info": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CheckpointHeader)]),
     "poe_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
-    "poe_tune_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
-    "poe_batch_tune_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
     "poe_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _fp]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "poe_reset_shot": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -78,7 +78,6 @@ struct poe_ctx {
     int ntx = 1, ntz = 1;       // tiles across x and z
     int order = POE_ORDER_BALANCED;   // work-list order (POE_ORDER_*)
     int graph_steps = kGraphSteps;   // steps per captured graph
-    int warp_groups = 1;             // compute-warp groups of the step kernel (1 or 2)
     int tile_x = PAL_TX, tile_z = PAL_TZ;
     poe_batch *batch = nullptr;   // the batch this context belongs to, if any
     uint64_t prof_hash = 0;       // of the C-PML profiles given to poe_create
@@ -352,7 +351,7 @@ int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
 int step_launch(poe_ctx *ctx, int k)
 {
     return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), ctx->items_dev, (int)ctx->items.size(), k,
-                            ctx->exact, ctx->kone, ctx->warp_groups, ctx->stream);
+                            ctx->exact, ctx->kone, ctx->stream);
 }
 
 int run_direct(poe_ctx *ctx, int64_t nsteps)
@@ -1126,15 +1125,6 @@ int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps)
     return POE_OK;
 }
 
-int poe_tune_kernel(poe_ctx *ctx, int32_t warp_groups)
-{
-    if (!ctx) return POE_EINVAL;
-    if (warp_groups != 1 && warp_groups != 2) return fail(ctx, POE_EINVAL, "tuning: warp_groups must be 1 or 2");
-    if (warp_groups != ctx->warp_groups) drop_graph(ctx);
-    ctx->warp_groups = warp_groups;
-    return POE_OK;
-}
-
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out)
 {
     if (!ctx || trial_steps < 1) return POE_EINVAL;
@@ -1248,7 +1238,6 @@ struct poe_batch {
     int device = 0;
     bool exact = true, kone = true, few = true;
     bool coef = false;          // the models read their coefficient planes per cell
-    int warp_groups = 1;        // compute-warp groups of the step kernel (1 or 2)
     ModelDev *models_dev = nullptr;
     StreamShot *shots_dev = nullptr;
     int4 *items_dev = nullptr;
@@ -1309,7 +1298,7 @@ int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
 {
     for (int64_t k = 0; k < nsteps; ++k) {
         const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->few,
-                                        b->coef, b->kone, b->warp_groups, b->stream);
+                                        b->coef, b->kone, b->stream);
         if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
     }
     const int r = launch_advance_shots(b->shots_dev, nshots, nsteps, b->stream);
@@ -1327,7 +1316,7 @@ cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
     int rc = 0;
     for (int k = 0; k < kGraphSteps && rc == 0; ++k)
         rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->few, b->coef, b->kone,
-                               b->warp_groups, b->stream);
+                               b->stream);
     if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -1381,7 +1370,6 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
     b->device = ctxs[0]->device;
     b->exact = ctxs[0]->exact;
     b->coef = ctxs[0]->ids == nullptr;
-    b->warp_groups = ctxs[0]->warp_groups;
     for (poe_ctx *c : b->ctxs) b->kone = b->kone && c->kone;   // K = 1 divides are exact: KONE=false is safe
     for (poe_ctx *c : b->ctxs) b->few = b->few && c->m.qx.few_bits && c->m.qz.few_bits;
     if (cudaSetDevice(b->device) != cudaSuccess) {
@@ -1470,18 +1458,6 @@ int poe_batch_run(poe_batch *b, const int64_t *nsteps)
         BK(cudaStreamWaitEvent(ctx->stream, b->done, 0));
         for (ShotHost &s : ctx->shots) s.steps += nsteps[i];
     }
-    return POE_OK;
-}
-
-int poe_batch_tune_kernel(poe_batch *b, int32_t warp_groups)
-{
-    if (!b) return POE_EINVAL;
-    if (warp_groups != 1 && warp_groups != 2) return bfail(b, POE_EINVAL, "tuning: warp_groups must be 1 or 2");
-    if (warp_groups != b->warp_groups) {
-        BK(cudaStreamSynchronize(b->stream));   // a graph still running holds the old kernel
-        drop_batch_graphs(b);
-    }
-    b->warp_groups = warp_groups;
     return POE_OK;
 }
 

@@ -129,14 +129,12 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0,
 // z-stencils of a column reuse the values of the rows before them in
 // registers.  Stress: 9 bands x 2 halves cover the 64 x 36 stress cells;
 // velocity: 8 bands x 2 halves cover the 60 x 32 tile, while the remaining
-// warps record the tile's receivers.
-//
-// GRP = 1: the 18 warps work every item together (one task each per phase)
-// and may run one item ahead of each other.  GRP = 2: two groups of 9 warps,
-// each owning one buffer and taking every other item (two tasks per warp per
-// phase), so one group's mid-item barrier and phase changes overlap the other
-// group's work.  Buffers are handed over with mbarriers (full: producer ->
-// compute, empty: compute -> producer); every wait is bounded.
+// two warps record the tile's receivers.  The warps may run one item ahead
+// of each other.  (Splitting them into two groups of 9 that each own one
+// buffer and alternate items, so that one group's mid-item barrier overlaps
+// the other's work, measured 20 % slower: each group then waits for its own
+// buffer's copies.)  Buffers are handed over with mbarriers (full: producer
+// -> compute, empty: compute -> producer); every wait is bounded.
 constexpr int PCT = 576;                           // compute threads: 18 warps
 constexpr int ROWS = 4;                            // consecutive rows per compute task
 constexpr int PNT = PCT + 32;                      // + the producer warp
@@ -175,14 +173,21 @@ constexpr int NST = 2 * ((QZ + 4) / ROWS);         // stress: 9 bands x 2 halves
 constexpr int NVT = 2 * (QZ / ROWS);               // velocity: 8 bands x 2 halves
 static_assert((QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT == 32 * NST, "task grid");
 
+// Global accesses through the pointers the producer resolved for an item
+// (read back from shared memory, so the compiler sees generic pointers):
+// stated as global, they take the global path and are not taken for possible
+// writes to the shared-memory tile, so later tile reads need not wait for them.
+__device__ __forceinline__ void gst(float *p, float v) { __stwb(p, v); }
+__device__ __forceinline__ float gld(const float *p) { return __ldca(p); }
+
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
 // 330-353): co = (rho m - rhof^2)/dt, c1,2 = co +- rho (eta/kappa)/2
 __device__ __forceinline__ void velocity_coef(const float *__restrict__ c, int64_t pl, float dt, float A, float B,
                                               float w0, float v0, float &w1, float &v1)
 {
-    const float rho = c[C_RHO * pl], rhof = c[C_RHOF * pl];
-    const float rsm = c[C_RSM * pl], eok = c[C_EOK * pl];
+    const float rho = gld(c + C_RHO * pl), rhof = gld(c + C_RHOF * pl);
+    const float rsm = gld(c + C_RSM * pl), eok = gld(c + C_EOK * pl);
     const float co = (rho * rsm - rhof * rhof) / dt;
     const float c1 = co + rho * eok * 0.5f;
     const float c2 = co - rho * eok * 0.5f;
@@ -221,36 +226,32 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // barrier 1: every compute warp
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(PCT) : "memory"); }
-// barrier 2 + g among the warps of group g only, returning whether v held in
-// every one of its threads
-template <int GRP>
-__device__ __forceinline__ bool group_sync_and(int g, bool v)
+// the same barrier, returning whether v held in every compute thread
+__device__ __forceinline__ bool compute_sync_and(bool v)
 {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "bar.red.and.pred q, 1, %2, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)v), "r"(2 + g), "n"(PCT / GRP)
+        : "r"((uint32_t)v), "n"(PCT)
         : "memory");
     return r != 0;
 }
 
 }  // namespace tile
 
-template <int SM, bool KONE, bool MULTI, bool COEF, int GRP>
+template <int SM, bool KONE, bool MULTI, bool COEF>
 __global__ void __launch_bounds__(tile::PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
            const int4 *__restrict__ items, int nitems, int k, int prefetch)
 {
     using namespace tile;
     constexpr bool EXACT = SM != SM_FAST;
-    constexpr int WPG = PCT / 32 / GRP;      // compute warps per group
-    constexpr int NVW = NVT / GRP;           // velocity warps per group (GRP tasks each); the rest record
-    static_assert(GRP == 1 || GRP == 2, "one or two warp groups");
-    static_assert(NST % WPG == 0 && NVT % GRP == 0 && WPG > NVW, "tasks divide among a group's warps");
+    constexpr int NW = PCT / 32;             // compute warps: one stress task each
+    static_assert(NST == NW && NW > NVT, "one stress task per warp; velocity warps, then receiver warps");
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     uint64_t *empty = full + 2;
@@ -259,7 +260,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
             mbar_init(&full[b], 1);
-            mbar_init(&empty[b], WPG);   // the warps of the group(s) computing from buffer b
+            mbar_init(&empty[b], NW);
         }
         mbar_fence_init();
     }
@@ -376,25 +377,26 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
 
     // ------------------------------------------------------------ compute
     const int wid = tid >> 5, lane = tid & 31;
-    const int grp = wid / WPG, gw = wid % WPG;    // group, warp in the group
-    const int gtid = tid - grp * WPG * 32;        // thread in the group
+    // this warp's stress task, which is also its velocity task if wid < NVT:
+    // column lx of the 64-wide stress tile, rows zb0 .. zb0+3
+    const int lx = (wid & 1) * 32 + lane, zb0 = (wid >> 1) * ROWS;
     if (!MULTI) {
         // single model: one material table for every item, in buffer 0's slot
         float *t0 = reinterpret_cast<float *>(smp + BUF_OFF_T);
         for (int i = tid; i < mp.nmat * MT_W; i += PCT) t0[i] = mp.mtab[i];
         compute_sync();
     }
-    int j = grp;
-    for (int w = blockIdx.x + grp * gridDim.x; w < nitems; w += GRP * gridDim.x, j += GRP) {
+    int j = 0;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
         const int b = j & 1;
         unsigned char *buf = smp + b * BUF_BYTES;
         // No barrier here: warps run ahead into the item as soon as its data
         // has landed.  A wait that gave up leaves the buffer's contents (item
         // parameters included) untrusted: touch nothing, join the item's
-        // mid-point barrier, which then ends every thread of the group together.
+        // mid-point barrier, which then ends every compute thread together.
         if (!mbar_wait(&full[b], (uint32_t)((j >> 1) & 1))) {
-            group_sync_and<GRP>(grp, false);
-            if (gtid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
+            compute_sync_and(false);
+            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
             return;
         }
         const ModelDev &m = MULTI ? *reinterpret_cast<const ModelDev *>(buf + BUF_OFF_MD) : mp;
@@ -431,75 +433,60 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             // exact zero; with FAST stencils the addition is skipped there (it
             // could only turn a -0 into +0), EXACT keeps the reference's sum.
             auto addm = [](float v, float mv) { return (SM == SM_FAST && IN) ? v : v + mv; };
-            // velocity tasks of this warp: t = gw + i NVW (lx, zb0 as below)
-            if (gw < NVW) {
+            if (wid < NVT) {
+                if (COEF && lx < QX) {
+                    // the density coefficients this thread's velocity rows read (rows
+                    // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
+                    const float *c = cf + (int64_t)(z0 + zb0 + ZH) * P + x0 + lx + XH;
 #pragma unroll
-                for (int i = 0; i < GRP; ++i) {
-                    const int t = gw + i * NVW;
-                    const int lx = (t & 1) * 32 + lane, zb0 = (t >> 1) * ROWS;
-                    if (COEF && lx < QX) {
-                        // the density coefficients this thread's velocity rows read (rows
-                        // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
-                        const float *c = cf + (int64_t)(z0 + zb0 + ZH) * P + x0 + lx + XH;
+                    for (int r = 0; r < ROWS + 1; ++r)
 #pragma unroll
-                        for (int r = 0; r < ROWS + 1; ++r)
-#pragma unroll
-                            for (int pl = C_RHO; pl <= C_EOK; ++pl)
-                                asm volatile("prefetch.global.L1 [%0];" ::"l"(c + pl * PL + (int64_t)r * P));
-                    }
-                    if (!IN && prefetch && lx < QX && x0 + lx <= NX) {
-                        // the velocity C-PML memory this thread updates in place after the
-                        // stress phase (rows zb0 .. zb0+3 of column lx, on the strips): to L1 now
-                        const int x = x0 + lx;
-                        const int xc = xcol(m, x);
-#pragma unroll
-                        for (int r = 0; r < ROWS; ++r) {
-                            const int tz = z0 + zb0 + r;
-                            if (tz > NZ) break;
-                            const int zr = zrow(m, tz);
-                            if (xc >= 0)
-#pragma unroll
-                                for (int a = 0; a < 3; ++a)
-                                    asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + tz * Wx + xc));
-                            if (zr >= 0)
-#pragma unroll
-                                for (int a = 0; a < 3; ++a)
-                                    asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
-                        }
-                    }
+                        for (int pl = C_RHO; pl <= C_EOK; ++pl)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(c + pl * PL + (int64_t)r * P));
                 }
-            }
-            if (!IN && prefetch) {
-                // the stress C-PML memory of this warp's stress rows: to L1 before
-                // the first row needs it
-#pragma unroll
-                for (int i = 0; i < NST / WPG; ++i) {
-                    const int t = gw + i * WPG;
-                    const int lx = (t & 1) * 32 + lane, zb0 = (t >> 1) * ROWS;
-                    const int x = x0 - 2 + lx;
-                    if (x < 0 || x > NX) continue;
+                if (!IN && prefetch && lx < QX && x0 + lx <= NX) {
+                    // the velocity C-PML memory this thread updates in place after the
+                    // stress phase (rows zb0 .. zb0+3 of column lx, on the strips): to L1 now
+                    const int x = x0 + lx;
                     const int xc = xcol(m, x);
 #pragma unroll
                     for (int r = 0; r < ROWS; ++r) {
-                        const int z = z0 - 2 + zb0 + r;
-                        if (z < 0 || z > NZ) continue;
-                        const int zr = zrow(m, z);
+                        const int tz = z0 + zb0 + r;
+                        if (tz > NZ) break;
+                        const int zr = zrow(m, tz);
                         if (xc >= 0)
 #pragma unroll
                             for (int a = 0; a < 3; ++a)
-                                asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxr + a * nzx + z * Wx + xc));
+                                asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + tz * Wx + xc));
                         if (zr >= 0)
 #pragma unroll
                             for (int a = 0; a < 3; ++a)
-                                asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzr + a * hzp + zr * P + x + XH));
+                                asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
                     }
                 }
             }
-            // ---- stress on the tile + 2-cell halo: per task, column lx, rows zb0 .. zb0+3
-#pragma unroll 1
-            for (int i = 0; i < NST / WPG; ++i) {
-                const int t = gw + i * WPG;
-                const int lx = (t & 1) * 32 + lane, zb0 = (t >> 1) * ROWS;
+            if (!IN && prefetch && x0 - 2 + lx >= 0 && x0 - 2 + lx <= NX) {
+                // the stress C-PML memory of this thread's stress rows: to L1 before
+                // the first row needs it
+                const int x = x0 - 2 + lx;
+                const int xc = xcol(m, x);
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int z = z0 - 2 + zb0 + r;
+                    if (z < 0 || z > NZ) continue;
+                    const int zr = zrow(m, z);
+                    if (xc >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxr + a * nzx + z * Wx + xc));
+                    if (zr >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzr + a * hzp + zr * P + x + XH));
+                }
+            }
+            // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
+            {
                 const int x = x0 - 2 + lx;
                 const bool x_ok = IN || (x >= 0 && x <= NX);
                 const bool x_g1 = IN || (x >= 1 && x <= NX - 1), x_g2 = IN || (x >= 2 && x <= NX - 1);
@@ -552,11 +539,11 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     float lc, mu, al, M, mu_top;
                     if (COEF) {
                         const float *c = cf + o;
-                        lc = c[C_LC * PL];
-                        mu = c[C_MU * PL];
-                        al = c[C_AL * PL];
-                        M = c[C_M * PL];
-                        mu_top = c[C_MU * PL + P];                   // rmu[top] (cu:218)
+                        lc = gld(c + C_LC * PL);
+                        mu = gld(c + C_MU * PL);
+                        al = gld(c + C_AL * PL);
+                        M = gld(c + C_M * PL);
+                        mu_top = gld(c + C_MU * PL + P);             // rmu[top] (cu:218)
                     } else {
                         const float4 ma = *reinterpret_cast<const float4 *>(st + MT_W * idc[r]);
                         mu_top = st[MT_W * idc[r + 1] + MT_MU];      // rmu[top] (cu:218)
@@ -570,26 +557,32 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (xc >= 0 && (g1 || g2)) {
                         const int ix = z * Wx + xc;
                         const float *MA = IM.mxr;
-                        m1 = bxh * MA[MXS_SXX * nzx + ix] + axh * vdx;
-                        m3 = bxh * MA[MXS_S2 * nzx + ix] + axh * wdx;
-                        m5 = bx * MA[MXS_SXZ * nzx + ix] + ax * sdx;
+                        m1 = bxh * gld(MA + MXS_SXX * nzx + ix) + axh * vdx;
+                        m3 = bxh * gld(MA + MXS_S2 * nzx + ix) + axh * wdx;
+                        m5 = bx * gld(MA + MXS_SXZ * nzx + ix) + ax * sdx;
                         if (own) {
                             float *MB = IM.mxw;
-                            if (g1) { MB[MXS_SXX * nzx + ix] = m1; MB[MXS_S2 * nzx + ix] = m3; }
-                            if (g2) MB[MXS_SXZ * nzx + ix] = m5;
+                            if (g1) {
+                                gst(MB + MXS_SXX * nzx + ix, m1);
+                                gst(MB + MXS_S2 * nzx + ix, m3);
+                            }
+                            if (g2) gst(MB + MXS_SXZ * nzx + ix, m5);
                         }
                     }
                     if (zr >= 0 && (g1 || g2)) {
                         const int iz = zr * P + xi;
                         const float *MA = IM.mzr;
                         const float bz = PZs[PB * PZH + pzo], az = PZs[PA * PZH + pzo];
-                        m2 = bz * MA[MZS_SXX * hzp + iz] + az * vdz;
-                        m4 = bz * MA[MZS_S2 * hzp + iz] + az * wdz;
-                        m6 = PZs[PBH * PZH + pzo] * MA[MZS_SXZ * hzp + iz] + PZs[PAH * PZH + pzo] * sdz;
+                        m2 = bz * gld(MA + MZS_SXX * hzp + iz) + az * vdz;
+                        m4 = bz * gld(MA + MZS_S2 * hzp + iz) + az * wdz;
+                        m6 = PZs[PBH * PZH + pzo] * gld(MA + MZS_SXZ * hzp + iz) + PZs[PAH * PZH + pzo] * sdz;
                         if (own) {
                             float *MB = IM.mzw;
-                            if (g1) { MB[MZS_SXX * hzp + iz] = m2; MB[MZS_S2 * hzp + iz] = m4; }
-                            if (g2) MB[MZS_SXZ * hzp + iz] = m6;
+                            if (g1) {
+                                gst(MB + MZS_SXX * hzp + iz, m2);
+                                gst(MB + MZS_S2 * hzp + iz, m4);
+                            }
+                            if (g2) gst(MB + MZS_SXZ * hzp + iz, m6);
                         }
                     }
                     const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo];
@@ -603,7 +596,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     const bool is_src = !IN && cell_ok && o == src_off;
                     if (is_src && !g1) pv = pacc;                    // sigma2 never overwritten there
                     if (is_src && src_where == SRC_P && src_on) pv = pv + src_val;   // cu:107-109
-                    if (is_src && own) *IM.acc_w = pv;
+                    if (is_src && own) gst(IM.acc_w, pv);
                     if (g2) {   // cu:223-226
                         const float Ssum = addm(addm(KDIV<KONE>(sdx, Kx), m5) + KDIV<KONE>(sdz, Kz), m6);
                         sxz = EXACT ? sxz_exact(sxz, mu_top, Ssum, dt) : sxz_fast(sxz, mu_top, Ssum, dt);
@@ -614,11 +607,11 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         else sxx_szz_fast(lc, mu, g11, g22, al, pv, sxx, szz);
                     }
                     if (own) {
-                        FB[SF_G11 * PL + o] = g11;
-                        FB[SF_G22 * PL + o] = g22;
-                        FB[SF_XI1 * PL + o] = xi1;
-                        FB[SF_XI2 * PL + o] = xi2;
-                        FB[SF_SXZ * PL + o] = sxz;
+                        gst(FB + SF_G11 * PL + o, g11);
+                        gst(FB + SF_G22 * PL + o, g22);
+                        gst(FB + SF_XI1 * PL + o, xi1);
+                        gst(FB + SF_XI2 * PL + o, xi2);
+                        gst(FB + SF_SXZ * PL + o, sxz);
                     }
                     // this thread alone reads these slots of this cell: outputs overwrite inputs
                     ss[PO_SXX * PS_FLOATS + so] = sxx;
@@ -627,31 +620,27 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ss[PO_SXZ * PS_FLOATS + so] = sxz;
                 }
             }
-            if (!group_sync_and<GRP>(grp, true)) return false;   // false: a thread's wait for this item gave up
+            if (!compute_sync_and(true)) return false;   // false: a thread's wait for this item gave up
 
-            if (gw >= NVW) {
+            if (wid >= NVT) {
                 // ---- receivers of this tile (vx, vz before the update; p of this step)
                 if (IM.nrec_q > 0) {
                     float *trace_row = IM.trace_row;
-                    for (int q = gtid - 32 * NVW; q < IM.nrec_q; q += 32 * (WPG - NVW)) {
+                    for (int q = tid - 32 * NVT; q < IM.nrec_q; q += PCT - 32 * NVT) {
                         const int4 Rq = IM.rec[q];               // (x, comp, slot, z)
                         const int xl = Rq.x - x0, zl = Rq.w - z0;
                         float v;
                         if (Rq.y == 2) v = ss[PO_P * PS_FLOATS + (zl + 2) * TMA_VW + xl + 4];
                         else v = sv[(Rq.y == 0 ? 0 : 1) * PV_FLOATS + (zl + 4) * TMA_VW + xl + 4];
-                        trace_row[Rq.z] = v;
+                        gst(trace_row + Rq.z, v);
                     }
                 }
                 return true;
             }
-            // ---- velocity on the tile: per task, column lx (< 60), rows zb0 .. zb0+3
+            // ---- velocity on the tile: column lx (< 60), rows zb0 .. zb0+3
             float *__restrict__ MXV = IM.mxv;
             float *__restrict__ MZV = IM.mzv;
-#pragma unroll 1
-            for (int i = 0; i < GRP; ++i) {
-                const int t = gw + i * NVW;
-                const int lx = (t & 1) * 32 + lane, zb0 = (t >> 1) * ROWS;
-                if (lx >= QX) continue;
+            if (lx < QX) {
                 const int x = x0 + lx;
                 const bool x_in = IN || x <= NX;
                 const bool x_vx = IN || (x >= 2 && x <= NX - 1), x_vz = IN || (x >= 1 && x <= NX - 2);   // cu:289, 326
@@ -700,22 +689,28 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         const int ix = tz * Wx + xc;
                         float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
                         float *M4 = MXV + MXV_VZ * nzx + ix;
-                        m1 = bx * *M1 + ax * d1x;
-                        m2 = bx * *M2 + ax * d2x;
-                        m4 = bxh * *M4 + axh * d1z;
-                        if (gvx) { *M1 = m1; *M2 = m2; }
-                        if (gvz) *M4 = m4;
+                        m1 = bx * gld(M1) + ax * d1x;
+                        m2 = bx * gld(M2) + ax * d2x;
+                        m4 = bxh * gld(M4) + axh * d1z;
+                        if (gvx) {
+                            gst(M1, m1);
+                            gst(M2, m2);
+                        }
+                        if (gvz) gst(M4, m4);
                     }
                     if (zr >= 0 && (gvx || gvz)) {
                         const int iz = zr * P + xi;
                         float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
                         float *M6 = MZV + MZV_VZ2 * hzp + iz;
                         const float bh = PZs[PBH * PZH + pzo], ah = PZs[PAH * PZH + pzo];
-                        m3 = PZs[PB * PZH + pzo] * *M3 + PZs[PA * PZH + pzo] * d3x;
-                        m5 = bh * *M5 + ah * d2z;
-                        m6 = bh * *M6 + ah * d3z;
-                        if (gvx) *M3 = m3;
-                        if (gvz) { *M5 = m5; *M6 = m6; }
+                        m3 = PZs[PB * PZH + pzo] * gld(M3) + PZs[PA * PZH + pzo] * d3x;
+                        m5 = bh * gld(M5) + ah * d2z;
+                        m6 = bh * gld(M6) + ah * d3z;
+                        if (gvx) gst(M3, m3);
+                        if (gvz) {
+                            gst(M5, m5);
+                            gst(M6, m6);
+                        }
                     }
                     const float Kz = KONE ? 1.0f : PZs[PK * PZH + pzo], Kzh = KONE ? 1.0f : PZs[PKH * PZH + pzo];
                     float vx1 = vx0, wx1 = wx0, vz1 = vz0, wz1 = wz0;
@@ -752,16 +747,16 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         }
                         if (gvz) { wz1 = w1; vz1 = v1; }
                     }
-                    FB[SF_VX * PL + o] = vx1;
-                    FB[SF_WX * PL + o] = wx1;
-                    FB[SF_VZ * PL + o] = vz1;
-                    FB[SF_WZ * PL + o] = wz1;
+                    gst(FB + SF_VX * PL + o, vx1);
+                    gst(FB + SF_WX * PL + o, wx1);
+                    gst(FB + SF_VZ * PL + o, vz1);
+                    gst(FB + SF_WZ * PL + o, wz1);
                 }
             }
             return true;
         };
         if (!(IM.interior ? compute(std::true_type{}) : compute(std::false_type{}))) {
-            if (gtid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
+            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
             return;
         }
         // hand buffer b back to the producer
@@ -794,12 +789,12 @@ inline int prefetch_strips(int nitems) { return nitems >= 8 * sm_count() ? 1 : 0
 
 // one launch of the step kernel of stencil mode SM: a single model (models
 // null) or a batch (models: device array; m unused)
-template <int SM, bool KONE, bool MULTI, bool COEF, int GRP>
+template <int SM, bool KONE, bool MULTI, bool COEF>
 int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
                 int k, cudaStream_t st)
 {
     static std::atomic<uint64_t> done{0};
-    auto kern = k_tile_pal<SM, KONE, MULTI, COEF, GRP>;
+    auto kern = k_tile_pal<SM, KONE, MULTI, COEF>;
     smem_attr_once(kern, (int)tile::PAL_SMEM, done);
     const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
     if (grid > 0) kern<<<grid, tile::PNT, tile::PAL_SMEM, st>>>(m, models, shots, items, nitems, k,
@@ -807,27 +802,22 @@ int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *sho
     return (int)cudaGetLastError();
 }
 
-// every (KONE, MULTI, COEF, GRP) variant of one stencil mode
+// every (KONE, MULTI, COEF) variant of one stencil mode
 template <int SM>
 int tile_launch_mode(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-                     int nitems, int k, bool kone, bool coef, int grp, cudaStream_t st)
+                     int nitems, int k, bool kone, bool coef, cudaStream_t st)
 {
     const bool multi = models != nullptr;
-    const int sel = (kone ? 8 : 0) | (multi ? 4 : 0) | (coef ? 2 : 0) | (grp == 2 ? 1 : 0);
-    switch (sel) {
-#define POE_TILE_CASE(s, KO, MU, CO, G) \
-    case s: return tile_launch<SM, KO, MU, CO, G>(m, models, shots, items, nitems, k, st);
-        POE_TILE_CASE(0, false, false, false, 1) POE_TILE_CASE(1, false, false, false, 2)
-        POE_TILE_CASE(2, false, false, true, 1) POE_TILE_CASE(3, false, false, true, 2)
-        POE_TILE_CASE(4, false, true, false, 1) POE_TILE_CASE(5, false, true, false, 2)
-        POE_TILE_CASE(6, false, true, true, 1) POE_TILE_CASE(7, false, true, true, 2)
-        POE_TILE_CASE(8, true, false, false, 1) POE_TILE_CASE(9, true, false, false, 2)
-        POE_TILE_CASE(10, true, false, true, 1) POE_TILE_CASE(11, true, false, true, 2)
-        POE_TILE_CASE(12, true, true, false, 1) POE_TILE_CASE(13, true, true, false, 2)
-        POE_TILE_CASE(14, true, true, true, 1) POE_TILE_CASE(15, true, true, true, 2)
-#undef POE_TILE_CASE
+    switch ((kone ? 4 : 0) | (multi ? 2 : 0) | (coef ? 1 : 0)) {
+    case 0: return tile_launch<SM, false, false, false>(m, models, shots, items, nitems, k, st);
+    case 1: return tile_launch<SM, false, false, true>(m, models, shots, items, nitems, k, st);
+    case 2: return tile_launch<SM, false, true, false>(m, models, shots, items, nitems, k, st);
+    case 3: return tile_launch<SM, false, true, true>(m, models, shots, items, nitems, k, st);
+    case 4: return tile_launch<SM, true, false, false>(m, models, shots, items, nitems, k, st);
+    case 5: return tile_launch<SM, true, false, true>(m, models, shots, items, nitems, k, st);
+    case 6: return tile_launch<SM, true, true, false>(m, models, shots, items, nitems, k, st);
+    default: return tile_launch<SM, true, true, true>(m, models, shots, items, nitems, k, st);
     }
-    return (int)cudaErrorInvalidValue;
 }
 
 }  // namespace poe

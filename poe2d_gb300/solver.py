@@ -237,11 +237,6 @@ class Solver:
         dealt for an even share of edge tiles per CTA) and graph length."""
         self._check(L.lib().poe_tune(self.h, int(order), int(graph_steps)))
 
-    def tune_kernel(self, warp_groups=1):
-        """Compute-warp groups of the step kernel: 1 (the 18 compute warps work
-        each tile together) or 2 (two groups of 9 alternate tiles)."""
-        self._check(L.lib().poe_tune_kernel(self.h, int(warp_groups)))
-
     def autotune(self, trial_steps=128):
         """Time the 8 (order, graph_steps) candidates, keep the fastest; shots must be
         at step 0 and are reset after.  Returns (order, graph_steps, ms per candidate)."""
@@ -326,11 +321,6 @@ class Batch:
     def sync(self):
         self._live()
         self._check(L.lib().poe_batch_sync(self.h))
-
-    def tune_kernel(self, warp_groups=1):
-        """Compute-warp groups of the batch's step kernel (see Solver.tune_kernel)."""
-        self._live()
-        self._check(L.lib().poe_batch_tune_kernel(self.h, int(warp_groups)))
 
     @property
     def launches(self):

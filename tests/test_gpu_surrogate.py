@@ -80,12 +80,13 @@ def test_params_roundtrip_and_training_fits_a_batch(poe):
 def test_adam_steps_match_numpy_adam(poe):
     """Three poe_sg_adam steps on gradients of three batches against numpy's
     Adam (oracle/surrogate_ref.py: bias-corrected moments, float64), each step
-    from the GPU's own state before it.  The moments m and v and the FP32
-    weights agree within 1e-6 of the magnitudes they are summed from (the
-    kernel folds the bias corrections into its step size and epsilon; its FP32
-    rounding is far below that bound, also where a sum cancels), the bf16
-    weight copy equals the FP32 weights rounded to nearest-even bit for bit,
-    and the step counter counts."""
+    from the GPU's own state before it.  The moments m and v agree within
+    1e-6 of the magnitudes they are summed from, and the FP32 weights within
+    1e-6 of |w| + |w_new| of numpy's update from the GPU's new moments (the
+    kernel folds the bias corrections into its step size and epsilon; its
+    FP32 rounding is far below those bounds, also where a sum cancels).  The
+    bf16 weight copy equals the FP32 weights rounded to nearest-even bit for
+    bit, and the step counter counts."""
     from oracle import surrogate_ref as R
     from poe2d_gb300.surrogate import Surrogate
     net = Surrogate(max_batch=8, seed=11)
@@ -101,15 +102,18 @@ def test_adam_steps_match_numpy_adam(poe):
         g = net.grads().astype(np.float64)
         assert np.count_nonzero(g) > 0.25 * g.size        # ReLU zeroes some units' gradients
         net.adam(lr)
-        w1, m1, v1 = R.adam_step(w, g, m, v, t, lr)
+        _, m1, v1 = R.adam_step(w, g, m, v, t, lr)
         gm, gv, w16, steps = net.state()
-        gw = net.params()
+        gw = net.params().astype(np.float64)
         assert steps == t
+        # the weights: numpy's update from the moments the GPU holds now
+        c1, c2 = 1.0 - b1 ** t, 1.0 - float(R.ADAM_B2) ** t
+        w1 = w - lr * (gm / c1) / (np.sqrt(gv / c2) + R.ADAM_EPS)
         bounds = (("m", gm, m1, b1 * np.abs(m) + one_b1 * np.abs(g)), ("v", gv, v1, np.abs(v1)),
                   ("w", gw, w1, np.abs(w) + np.abs(w1)))
         for name, a, b, mag in bounds:
-            err = np.abs(a.astype(np.float64) - b)
+            err = np.abs(np.asarray(a, np.float64) - b)
             assert np.all(err <= 1e-6 * mag + 1e-37), (t, name, float((err / (mag + 1e-37)).max()))
-        assert np.array_equal(w16.view(np.uint32), R.bf16_bits(gw)), t
-        w, m, v = gw.astype(np.float64), gm.astype(np.float64), gv.astype(np.float64)
+        assert np.array_equal(w16.view(np.uint32), R.bf16_bits(gw.astype(np.float32))), t
+        w, m, v = gw, gm.astype(np.float64), gv.astype(np.float64)
     net.close()

@@ -3,14 +3,13 @@
 
 The step kernel runs 608 threads per CTA (18 compute warps + 1 producer) at
 one CTA per SM, so ptxas caps it at 96 registers; what does not fit goes to
-local memory.  With one warp group, the single-model variants and the batch
-variants the batched benchmarks run (palette models with K = 1, FAST or
-few-bit EXACT stencils) must not spill, nor may the two-group variant of the
-benchmarked single-model path (FAST, K = 1, palette).  The remaining variants
-(K != 1, per-cell coefficients, EXACT at a spacing whose 24 h needs more than
-8 bits, two warp groups) spill a few dozen bytes per thread to L1-resident
-local memory; the bound below keeps that from growing unnoticed.  The
-surrogate kernels must not spill either.
+local memory.  The single-model variants and the batch variants the batched
+benchmarks run (palette models with K = 1, FAST or few-bit EXACT stencils)
+must not spill.  The remaining batch variants (K != 1, per-cell
+coefficients, or EXACT at a spacing whose 24 h needs more than 8 bits) spill
+a few dozen bytes per thread to L1-resident local memory; the bound below
+keeps that from growing unnoticed.  The surrogate kernels must not spill
+either.
 """
 import os
 import re
@@ -61,27 +60,26 @@ def _step_variants(reports):
     out = {}
     for unit in TILE_UNITS:
         for name, res in reports[unit].items():
-            m = re.search(r"k_tile_palILi(\d)ELb(\d)ELb(\d)ELb(\d)ELi(\d)E", name)
+            m = re.search(r"k_tile_palILi(\d)ELb(\d)ELb(\d)ELb(\d)E", name)
             if m:
-                sm, kone, multi, coef, grp = (int(v) for v in m.groups())
-                out[(MODES[sm], bool(kone), bool(multi), bool(coef), grp)] = res
+                sm, kone, multi, coef = (int(v) for v in m.groups())
+                out[(MODES[sm], bool(kone), bool(multi), bool(coef))] = res
     return out
 
 
 def test_every_step_kernel_variant_is_built(reports):
     v = _step_variants(reports)
-    assert len(v) == 3 * 2 * 2 * 2 * 2, sorted(v)
+    assert len(v) == 3 * 2 * 2 * 2, sorted(v)
     for key, (regs, _, _, _) in v.items():
         assert regs <= 96, (key, regs)   # 608 threads at one CTA per SM
 
 
 def test_single_model_and_benchmarked_batch_variants_do_not_spill(reports):
     v = _step_variants(reports)
-    for (mode, kone, multi, coef, grp), (regs, stack, st, ld) in v.items():
-        key = (mode, kone, multi, coef, grp)
+    for key, (regs, stack, st, ld) in v.items():
+        mode, kone, multi, coef = key
         benchmarked_batch = multi and kone and not coef and mode in ("FAST", "EXACT_FEW")
-        benchmarked_single = not multi and kone and not coef and mode == "FAST"
-        if (grp == 1 and (not multi or benchmarked_batch)) or benchmarked_single:
+        if not multi or benchmarked_batch:
             assert st == 0 and ld == 0, (key, st, ld)
         else:
             assert st <= 128 and ld <= 256, (key, st, ld)

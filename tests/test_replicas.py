@@ -77,3 +77,61 @@ def test_two_gloo_ranks_shard_and_gather():
     assert keys == [0, 1, 2, 3, 4]
     assert all(v > 0 for v in merged.values())
     assert t == 2.0
+
+
+def _oracle_solve(specs):
+    """What gpu_solve does on a GPU, on the CPU oracle: each spec's model
+    (datagen.build_model with a thin C-PML and 8 receivers) for its steps."""
+    from oracle import oracle as O
+    from poe2d_gb300 import datagen as D
+    out = {}
+    for sp in specs:
+        g, coef, px, pz, src, rec, _ = D.build_model(sp, npml=4, nrec=8)
+        o = O.Oracle(O.F32, g.NX, g.NZ, g.dx, g.dz, g.dt, coef, px, pz, threads=1)
+        o.set_source(src.ix, src.iz, O.SRC_FZ, O.source_table(1, src.f0, g.dt, sp["steps"], amplitude=src.amplitude,
+                                                              t_cut=0.0, dx=g.dx, dz=g.dz))
+        o.set_receivers(rec)
+        out[sp["index"]] = o.run(sp["steps"])
+    return out
+
+
+def _runner_rank(rank, world, port, q):
+    import torch.distributed as dist
+    from poe2d_gb300 import batch_runner as BR
+    from poe2d_gb300 import datagen as D
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    specs = D.uneven_specs(3, 7, n_min=24, n_max=44)
+    mine = shard([BR.cost(sp) for sp in specs], world)[rank]
+    merged, el = BR.run(specs, _oracle_solve)
+    q.put((rank, mine, None if merged is None else {k: v.tolist() for k, v in merged.items()}, el))
+    dist.destroy_process_group()
+
+
+def test_batch_runner_shards_models_over_two_ranks():
+    """The uneven-batch runner on two gloo ranks: every model is solved by
+    exactly one rank (the LPT shard), rank 0 receives every model's traces
+    and they equal a one-process run of the same models."""
+    import torch.multiprocessing as mp
+    from poe2d_gb300 import datagen as D
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_runner_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=240) for _ in range(2)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    by_rank = {r: (mine, merged, el) for r, mine, merged, el in got}
+    assert sorted(by_rank[0][0] + by_rank[1][0]) == list(range(7)) and by_rank[0][0] and by_rank[1][0]
+    assert by_rank[1][1] is None and by_rank[0][2] == by_rank[1][2] > 0     # the slowest rank's time on both
+    merged = by_rank[0][1]
+    specs = D.uneven_specs(3, 7, n_min=24, n_max=44)
+    want = _oracle_solve(specs)
+    assert sorted(merged) == list(range(7))
+    for k, v in want.items():
+        assert np.array_equal(np.asarray(merged[k], np.float32), v), k
+        assert np.abs(v).max() > 0
