@@ -413,6 +413,37 @@ def cpu_sample(g, coef, px, pz, src_ix, src_iz, target_s=12.0):
             "sample": "%d of the %d steps of the 2001x2001 shot (after 4 untimed), %.1f s" % (n, NSTEPS, el)}
 
 
+def padded_ids(n=2010, seed=0):
+    """The benchmark model's patchy ids on the n x n grid the reference's own
+    programs need (a multiple of 10 cells per side, cu:1597-1600)."""
+    from poe2d_gb300.patchy import random_patches
+    return random_patches((n, n), DX, fraction=0.10, r_min=2.0, r_max=10.0, seed=1234 + seed)
+
+
+def reference_gpu_leg():
+    """The reference's own CUDA program (staged by baseline/stage_ref.sh) on
+    this GPU, 2000 steps of the benchmark model padded to 2010 x 2010."""
+    from baseline import ref_programs as R
+    if not R.staged():
+        return {"unavailable": "the reference's sources are not staged (baseline/stage_ref.sh needs the reference tree)"}
+    try:
+        return R.time_cuda(padded_ids(), DX, DT, NPML, F0, nstep=2000, samp=1000)
+    except Exception as exc:                       # reported, never fatal to the bench line
+        return {"unavailable": repr(exc)[:300]}
+
+
+def reference_cpu_program_leg():
+    """The reference's own serial C++ program on one host core, one chunk of
+    51 steps of the benchmark model padded to 2010 x 2010."""
+    from baseline import ref_programs as R
+    if not R.staged():
+        return {"unavailable": "the reference's sources are not staged (baseline/stage_ref.sh needs the reference tree)"}
+    try:
+        return R.time_cpu(padded_ids(), DX, DT, NPML, F0, samp=50)
+    except Exception as exc:
+        return {"unavailable": repr(exc)[:300]}
+
+
 def bench_config(ids, ws):
     """The workload both arms report (the same dict for ours and the reference)."""
     return {"workload": "2001x2001 patchy gas/water sandstone shot, h=0.5 m, 40-cell C-PML, dt=5e-5 s, "
@@ -451,6 +482,7 @@ def run_reference(args, ws, rank):
     sample = ("%d bench steps, each a ~5 s sample (~%d of the %d time steps of the 2001x2001 shot), %.1f s total; "
               "the full shot would take %.0f s" % (args.steps, tot_n // max(args.steps, 1), NSTEPS, tot_t,
                                                      c.cells * NSTEPS / (value * 1e9)))
+    ref_prog = reference_cpu_program_leg() if not args.no_ref_programs else None
     line = {"metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot_t / max(args.steps, 1), "higher_is_better": True,
@@ -460,6 +492,7 @@ def run_reference(args, ws, rank):
                    "that builds), OpenMP over all host threads",
             "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": c.th, "kind": "port",
                              "sample": sample},
+            "reference_cpu_program": ref_prog,
             "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -476,6 +509,8 @@ def main():
                     help="fast: plain FP32 stencils; exact: FP32 arithmetic rounded like the reference's FP64 lines")
     ap.add_argument("--no-parity", action="store_true", help="skip the fast-vs-exact drift check")
     ap.add_argument("--no-orders", action="store_true", help="skip the work-list order comparison")
+    ap.add_argument("--no-ref-programs", action="store_true",
+                    help="skip timing the reference's own CUDA (ours) and serial C++ (reference arm) programs")
     ap.add_argument("--no-surrogate-train", action="store_true",
                     help="skip training and scoring the surrogate ensemble on its narrow family")
     ap.add_argument("--batched", type=int, default=64, metavar="M",
@@ -627,6 +662,9 @@ def main():
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_sample(g, coef, px, pz, src.ix, src.iz)
+    ref_gpu = None
+    if rank == 0 and ws == 1 and not args.no_ref_programs:
+        ref_gpu = reference_gpu_leg()
 
     if rank == 0:
         line = {
@@ -642,7 +680,7 @@ def main():
                          "algorithmic_bytes_per_step": alg, "step_us": step_s * 1e6,
                          "palette_min_bytes_per_step": alg_pal,
                          "palette_frac": alg_pal / step_s / 1e9 / hbm},
-            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": launches,
+            "cpu_baseline": cb, "reference_gpu": ref_gpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity, "batched": batched,
             "surrogate": surrogate, "orders": orders,
         }
