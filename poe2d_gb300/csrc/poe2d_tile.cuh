@@ -433,6 +433,34 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             // exact zero; with FAST stencils the addition is skipped there (it
             // could only turn a -0 into +0), EXACT keeps the reference's sum.
             auto addm = [](float v, float mv) { return (SM == SM_FAST && IN) ? v : v + mv; };
+            // The velocity C-PML memory this thread updates in place after the
+            // barrier (rows zb0 .. zb0+3 of column lx, on the strips), to L1.  A
+            // single model prefetches it just before the barrier, while the other
+            // warps finish their stress rows: prefetched at the tile start together
+            // with the stress phase's memory it overflows the L1 that the tile
+            // buffers leave (about 28 KB beside 205 KB of shared memory).  The
+            // batch kernel prefetches it at the tile start, where it spills no
+            // registers.
+            auto prefetch_velocity_memory = [&]() {
+                if (IN || !prefetch || wid >= NVT || lx >= QX || x0 + lx > NX) return;
+                const int x = x0 + lx;
+                const int xc = xcol(m, x);
+#pragma unroll
+                for (int r = 0; r < ROWS; ++r) {
+                    const int tz = z0 + zb0 + r;
+                    if (tz > NZ) break;
+                    const int zr = zrow(m, tz);
+                    if (xc >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + tz * Wx + xc));
+                    if (zr >= 0)
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
+                }
+            };
+            if (MULTI) prefetch_velocity_memory();
             if (COEF && wid < NVT && lx < QX) {
                 // the density coefficients this thread's velocity rows read (rows
                 // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
@@ -598,29 +626,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ss[PO_SXZ * PS_FLOATS + so] = sxz;
                 }
             }
-            if (!IN && prefetch && wid < NVT && lx < QX && x0 + lx <= NX) {
-                // the velocity C-PML memory this thread updates in place after the
-                // barrier (rows zb0 .. zb0+3 of column lx, on the strips): to L1 now, while
-                // the other warps finish their stress rows.  Prefetched at the tile start
-                // together with the stress phase's memory it overflows the L1 that the
-                // tile buffers leave (about 28 KB beside 205 KB of shared memory).
-                const int x = x0 + lx;
-                const int xc = xcol(m, x);
-#pragma unroll
-                for (int r = 0; r < ROWS; ++r) {
-                    const int tz = z0 + zb0 + r;
-                    if (tz > NZ) break;
-                    const int zr = zrow(m, tz);
-                    if (xc >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + tz * Wx + xc));
-                    if (zr >= 0)
-#pragma unroll
-                        for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
-                }
-            }
+            if (!MULTI) prefetch_velocity_memory();
             if (!compute_sync_and(true)) return false;   // false: a thread's wait for this item gave up
 
             if (wid >= NVT) {
