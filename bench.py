@@ -498,6 +498,7 @@ def run_reference(args, ws, rank):
 
 
 def main():
+    global NPML
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -509,6 +510,8 @@ def main():
                     help="fast: plain FP32 stencils; exact: FP32 arithmetic rounded like the reference's FP64 lines")
     ap.add_argument("--no-parity", action="store_true", help="skip the fast-vs-exact drift check")
     ap.add_argument("--no-orders", action="store_true", help="skip the work-list order comparison")
+    ap.add_argument("--pml", type=int, default=40,
+                    help="C-PML width in cells of the single-shot workload (profiling; the benchmark is 40)")
     ap.add_argument("--no-ref-programs", action="store_true",
                     help="skip timing the reference's own CUDA (ours) and serial C++ (reference arm) programs")
     ap.add_argument("--no-surrogate-train", action="store_true",
@@ -517,6 +520,7 @@ def main():
                     help="batched legs: 64 shots of one 1001x1001 model, and M of the 256 uneven models "
                          "(0 skips both)")
     args = ap.parse_args()
+    NPML = args.pml
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -583,7 +587,7 @@ def main():
     achieved = alg / step_s / 1e9
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+        with open(os.path.join(ROOT, "profiles", "k_tile_pal_traffic_2001x2001.json")) as f:
             tr = json.load(f)
         traffic = float(tr["dram_bytes_per_cell_update"]) * cells
     except Exception:
