@@ -7,8 +7,8 @@ stencils (plain FP32), and the oracle runs the same inputs in F64 on the host
 cores.  One JSON line per shot gives the relative L2 error of the traces
 against F64 and the largest trace error relative to the trace peak.
 
-    python tests/fp64_drift.py                                     # all four
-    python tests/fp64_drift.py --workloads sandstone201,shots1001  # a subset
+    python oracle/fp64_drift.py                                     # all four
+    python oracle/fp64_drift.py --workloads sandstone201,shots1001  # a subset
 
 Workloads (synthetic, seeded):
   sandstone201  201 x 201 homogeneous water-saturated sandstone, 20-cell

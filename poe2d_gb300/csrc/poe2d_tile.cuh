@@ -179,6 +179,10 @@ static_assert((QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT == 32 * NST, "task g
 // writes to the shared-memory tile, so later tile reads need not wait for them.
 __device__ __forceinline__ void gst(float *p, float v) { __stwb(p, v); }
 __device__ __forceinline__ float gld(const float *p) { return __ldca(p); }
+// data no thread writes during the launch (the previous step's stress C-PML
+// memory): non-coherent loads, which the compiler may issue ahead of earlier
+// stores since they cannot alias them
+__device__ __forceinline__ float gld_ro(const float *p) { return __ldg(p); }
 
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
@@ -563,9 +567,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (xc >= 0 && (g1 || g2)) {
                         const int ix = z * Wx + xc;
                         const float *MA = IM.mxr;
-                        m1 = bxh * gld(MA + MXS_SXX * nzx + ix) + axh * vdx;
-                        m3 = bxh * gld(MA + MXS_S2 * nzx + ix) + axh * wdx;
-                        m5 = bx * gld(MA + MXS_SXZ * nzx + ix) + ax * sdx;
+                        m1 = bxh * gld_ro(MA + MXS_SXX * nzx + ix) + axh * vdx;
+                        m3 = bxh * gld_ro(MA + MXS_S2 * nzx + ix) + axh * wdx;
+                        m5 = bx * gld_ro(MA + MXS_SXZ * nzx + ix) + ax * sdx;
                         if (own) {
                             float *MB = IM.mxw;
                             if (g1) {
@@ -579,9 +583,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         const int iz = zr * P + xi;
                         const float *MA = IM.mzr;
                         const float bz = PZs[PB * PZH + pzo], az = PZs[PA * PZH + pzo];
-                        m2 = bz * gld(MA + MZS_SXX * hzp + iz) + az * vdz;
-                        m4 = bz * gld(MA + MZS_S2 * hzp + iz) + az * wdz;
-                        m6 = PZs[PBH * PZH + pzo] * gld(MA + MZS_SXZ * hzp + iz) + PZs[PAH * PZH + pzo] * sdz;
+                        m2 = bz * gld_ro(MA + MZS_SXX * hzp + iz) + az * vdz;
+                        m4 = bz * gld_ro(MA + MZS_S2 * hzp + iz) + az * wdz;
+                        m6 = PZs[PBH * PZH + pzo] * gld_ro(MA + MZS_SXZ * hzp + iz) + PZs[PAH * PZH + pzo] * sdz;
                         if (own) {
                             float *MB = IM.mzw;
                             if (g1) {
