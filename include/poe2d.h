@@ -295,11 +295,22 @@ enum {
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 
-/* Time every (order, graph_steps in {16, 64}) pair on this context for
- * trial_steps steps, keep the fastest and report it; ms_out (may be NULL)
- * receives the POE_AUTOTUNE_CANDIDATES timings, order-major.  Every shot
- * must be at step 0; the shots are reset to step 0 afterwards. */
-enum { POE_AUTOTUNE_CANDIDATES = 8 };
+/* Step-spanning launches (no reference counterpart): span = 1 (the
+ * default) runs the graph_steps steps of each captured graph as ONE
+ * persistent launch, in which a tile of step n starts as soon as its 3 x 3
+ * neighbourhood of tiles has completed step n-1 (per-tile flags in device
+ * memory, bounded waits), so the steps overlap instead of each ending on its
+ * slowest CTA; span = 0 launches the step kernel once per step.  Results do
+ * not depend on it. */
+int poe_tune_span(poe_ctx *ctx, int32_t span);
+
+/* Time every (order, graph_steps in {16, 64}, span in {0, 1}) candidate on
+ * this context for trial_steps steps, keep the fastest and report it;
+ * ms_out (may be NULL) receives the POE_AUTOTUNE_CANDIDATES timings,
+ * candidate c = order c / 4, graph_steps {16, 64}[(c / 2) % 2], span c % 2.
+ * Every shot must be at step 0; the shots are reset to step 0 afterwards;
+ * poe_tune and poe_tune_span then hold the winner. */
+enum { POE_AUTOTUNE_CANDIDATES = 16 };
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out);
 
 /* Steps completed by a shot. */
@@ -341,6 +352,10 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
  * after the batch on a context's own stream (poe_get_traces, poe_run) is
  * ordered after it. */
 int poe_batch_run(poe_batch *b, const int64_t *nsteps);
+
+/* Step-spanning launches for the batch (poe_tune_span; a new batch takes its
+ * first context's setting). */
+int poe_batch_tune_span(poe_batch *b, int32_t span);
 
 /* Wait for the batch; POE_ETIMEOUT if a kernel's bounded wait gave up. */
 int poe_batch_sync(poe_batch *b);

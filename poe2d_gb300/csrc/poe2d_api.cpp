@@ -46,6 +46,7 @@ struct ShotHost {
     int src_where = SRC_NONE;
     int64_t steps = 0;
     uint64_t rec_hash = 0;   // of the receiver list (checkpoint identity)
+    int *done = nullptr;     // per tile: a step it has completed (step-spanning launches)
 };
 
 struct poe_ctx {
@@ -78,6 +79,7 @@ struct poe_ctx {
     int ntx = 1, ntz = 1;       // tiles across x and z
     int order = POE_ORDER_BALANCED;   // work-list order (POE_ORDER_*)
     int graph_steps = kGraphSteps;   // steps per captured graph
+    bool span = true;                // a step-spanning launch per graph (else one launch per step)
     int tile_x = PAL_TX, tile_z = PAL_TZ;
     poe_batch *batch = nullptr;   // the batch this context belongs to, if any
     uint64_t prof_hash = 0;       // of the C-PML profiles given to poe_create
@@ -147,6 +149,7 @@ void free_shot(ShotHost &s)
     cudaFree(s.trace);
     cudaFree(s.rec_start);
     cudaFree(s.rec_sorted);
+    cudaFree(s.done);
     s = ShotHost{};
 }
 
@@ -238,6 +241,7 @@ int sync_shots(poe_ctx *ctx)
         d.trace_cap = s.trace_cap;
         d.tm_v = s.tm ? (const void *)&s.tm[0] : nullptr;
         d.tm_s = s.tm ? (const void *)&s.tm[1] : nullptr;
+        d.done = s.done;
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
     }
@@ -348,19 +352,35 @@ int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
     return POE_OK;
 }
 
-int step_launch(poe_ctx *ctx, int k)
+// steps k .. k+nk-1 in one launch (nk > 1: step-spanning)
+int step_launch(poe_ctx *ctx, int k, int nk)
 {
     return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), ctx->items_dev, (int)ctx->items.size(), k,
-                            ctx->exact, ctx->kone, ctx->stream);
+                            nk, ctx->exact, ctx->kone, ctx->stream);
+}
+
+// the context's launches for nsteps steps (one step-spanning launch, or one
+// per step); returns the launches issued, or -1 with ctx->err set
+int64_t issue_steps(poe_ctx *ctx, int64_t nsteps)
+{
+    if (ctx->span && nsteps > 1) {
+        const int r = step_launch(ctx, 0, (int)nsteps);
+        if (r) return fail(ctx, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r)), -1;
+        return 1;
+    }
+    for (int64_t k = 0; k < nsteps; ++k) {
+        const int r = step_launch(ctx, (int)k, 1);
+        if (r) return fail(ctx, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r)), -1;
+    }
+    return nsteps;
 }
 
 int run_direct(poe_ctx *ctx, int64_t nsteps)
 {
     const int ns = (int)ctx->shots.size();
-    for (int64_t k = 0; k < nsteps; ++k) {
-        CKL(step_launch(ctx, (int)k));
-        ctx->launches += 1;
-    }
+    const int64_t l = issue_steps(ctx, nsteps);
+    if (l < 0) return POE_ECUDA;
+    ctx->launches += l;
     CKL(launch_advance(ctx->steps_dev, ns, nsteps, ctx->stream));
     ctx->launches += 1;
     return POE_OK;
@@ -372,8 +392,8 @@ int build_graph(poe_ctx *ctx)
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
-    for (int k = 0; k < ctx->graph_steps && rc == 0; ++k)
-        rc = step_launch(ctx, k);
+    const int64_t l = issue_steps(ctx, ctx->graph_steps);
+    if (l < 0) rc = (int)cudaErrorLaunchFailure;
     if (rc == 0) rc = launch_advance(ctx->steps_dev, ns, ctx->graph_steps, ctx->stream);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -387,7 +407,7 @@ int build_graph(poe_ctx *ctx)
         ctx->graph = nullptr;
         return fail(ctx, POE_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
-    ctx->graph_kernels = ctx->graph_steps + 1;   // one step kernel per step, one clock advance
+    ctx->graph_kernels = (int)l + 1;   // the step launches and one clock advance
     return POE_OK;
 }
 
@@ -608,6 +628,7 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     ctx->ntx = (nx + ctx->tile_x - 1) / ctx->tile_x;
     ctx->ntz = (nz + ctx->tile_z - 1) / ctx->tile_z;
     ctx->m.ntx = ctx->ntx;
+    ctx->m.ntz = ctx->ntz;
     *out = ctx;
     return POE_OK;
 }
@@ -694,6 +715,8 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     }
     if ((e = cudaMalloc(&s.acc, sizeof(float) * 2)) != cudaSuccess) return bad(e, "acc");
     if ((e = cudaMemsetAsync(s.acc, 0, sizeof(float) * 2, ctx->stream)) != cudaSuccess) return bad(e, "acc");
+    if ((e = cudaMalloc(&s.done, sizeof(int) * ncell)) != cudaSuccess) return bad(e, "tile flags");
+    if ((e = cudaMemsetAsync(s.done, 0, sizeof(int) * ncell, ctx->stream)) != cudaSuccess) return bad(e, "tile flags");
     if ((e = cudaMalloc(&s.rec_start, sizeof(int) * start.size())) != cudaSuccess) return bad(e, "receivers");
     if ((e = cudaMemcpyAsync(s.rec_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice,
                              ctx->stream)) != cudaSuccess)
@@ -884,6 +907,7 @@ int poe_reset_shot(poe_ctx *ctx, int32_t shot)
     if (s->mxv) CK(cudaMemsetAsync(s->mxv, 0, xbytes, ctx->stream));
     if (s->mzv) CK(cudaMemsetAsync(s->mzv, 0, zbytes, ctx->stream));
     CK(cudaMemsetAsync(s->acc, 0, sizeof(float) * 2, ctx->stream));
+    CK(cudaMemsetAsync(s->done, 0, sizeof(int) * ctx->ntx * ctx->ntz, ctx->stream));   // never ahead of the shot
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(float) * s->trace_cap * s->nrec, ctx->stream));
     s->steps = 0;
     ctx->shots_dirty = true;
@@ -1125,6 +1149,15 @@ int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps)
     return POE_OK;
 }
 
+int poe_tune_span(poe_ctx *ctx, int32_t span)
+{
+    if (!ctx) return POE_EINVAL;
+    if (span != 0 && span != 1) return fail(ctx, POE_EINVAL, "tuning: span must be 0 or 1");
+    if ((span != 0) != ctx->span) drop_graph(ctx);
+    ctx->span = span != 0;
+    return POE_OK;
+}
+
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out)
 {
     if (!ctx || trial_steps < 1) return POE_EINVAL;
@@ -1138,9 +1171,10 @@ int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t 
     CK(cudaEventCreate(&e1));
     int best = -1, rc = POE_OK;
     float best_ms = 0.0f;
+    // candidate c: order c / 4, graph length kSteps[(c / 2) % 2], span c % 2
     for (int c = 0; c < POE_AUTOTUNE_CANDIDATES && rc == POE_OK; ++c) {
-        const int order = c / 2, gs = kSteps[c % 2];
-        if ((rc = poe_tune(ctx, order, gs)) != POE_OK) break;
+        const int order = c / 4, gs = kSteps[(c / 2) % 2], span = c % 2;
+        if ((rc = poe_tune(ctx, order, gs)) != POE_OK || (rc = poe_tune_span(ctx, span)) != POE_OK) break;
         if ((rc = poe_run(ctx, gs)) != POE_OK) break;        // capture the graph, first touch
         cudaEventRecord(e0, ctx->stream);
         if ((rc = poe_run(ctx, trial_steps)) != POE_OK) break;
@@ -1162,9 +1196,10 @@ int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != POE_OK) return rc;
-    rc = poe_tune(ctx, best / 2, kSteps[best % 2]);
-    if (order_out) *order_out = best / 2;
-    if (graph_steps_out) *graph_steps_out = kSteps[best % 2];
+    if ((rc = poe_tune(ctx, best / 4, kSteps[(best / 2) % 2])) != POE_OK) return rc;
+    rc = poe_tune_span(ctx, best % 2);
+    if (order_out) *order_out = best / 4;
+    if (graph_steps_out) *graph_steps_out = kSteps[(best / 2) % 2];
     return rc;
 }
 
@@ -1238,6 +1273,7 @@ struct poe_batch {
     int device = 0;
     bool exact = true, kone = true, few = true;
     bool coef = false;          // the models read their coefficient planes per cell
+    bool span = true;           // a step-spanning launch per graph (else one launch per step)
     ModelDev *models_dev = nullptr;
     StreamShot *shots_dev = nullptr;
     int4 *items_dev = nullptr;
@@ -1294,16 +1330,27 @@ int grow(poe_batch *b, T **p, int &cap, int need)
     return POE_OK;
 }
 
+// the batch's launches for nsteps steps over the first nitems items (one
+// step-spanning launch, or one per step); returns the launches or -1
+int64_t batch_issue(poe_batch *b, int nitems, int64_t nsteps)
+{
+    const bool span = b->span && nsteps > 1;
+    const int64_t nl = span ? 1 : nsteps;
+    for (int64_t k = 0; k < nl; ++k) {
+        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k,
+                                        span ? (int)nsteps : 1, b->exact, b->few, b->coef, b->kone, b->stream);
+        if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r)), -1;
+    }
+    return nl;
+}
+
 int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
 {
-    for (int64_t k = 0; k < nsteps; ++k) {
-        const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k, b->exact, b->few,
-                                        b->coef, b->kone, b->stream);
-        if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
-    }
+    const int64_t l = batch_issue(b, nitems, nsteps);
+    if (l < 0) return POE_ECUDA;
     const int r = launch_advance_shots(b->shots_dev, nshots, nsteps, b->stream);
     if (r) return bfail(b, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r));
-    b->launches += nsteps + 1;
+    b->launches += l + 1;
     return POE_OK;
 }
 
@@ -1313,10 +1360,7 @@ cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
         if (b->graph_keys[i][0] == nitems && b->graph_keys[i][1] == nshots) return b->graphs[i];
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
-    int rc = 0;
-    for (int k = 0; k < kGraphSteps && rc == 0; ++k)
-        rc = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, k, b->exact, b->few, b->coef, b->kone,
-                               b->stream);
+    int rc = batch_issue(b, nitems, kGraphSteps) < 0 ? 1 : 0;
     if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -1340,7 +1384,7 @@ int batch_segment(poe_batch *b, int nitems, int nshots, int64_t nsteps)
         if (!g) return bfail(b, POE_ECUDA, "batch graph capture failed");
         for (; left >= kGraphSteps; left -= kGraphSteps) {
             BK(cudaGraphLaunch(g, b->stream));
-            b->launches += kGraphSteps + 1;
+            b->launches += (b->span ? 1 : kGraphSteps) + 1;
         }
     }
     return left > 0 ? batch_steps(b, nitems, nshots, left) : POE_OK;
@@ -1370,6 +1414,7 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
     b->device = ctxs[0]->device;
     b->exact = ctxs[0]->exact;
     b->coef = ctxs[0]->ids == nullptr;
+    b->span = ctxs[0]->span;
     for (poe_ctx *c : b->ctxs) b->kone = b->kone && c->kone;   // K = 1 divides are exact: KONE=false is safe
     for (poe_ctx *c : b->ctxs) b->few = b->few && c->m.qx.few_bits && c->m.qz.few_bits;
     if (cudaSetDevice(b->device) != cudaSuccess) {
@@ -1458,6 +1503,18 @@ int poe_batch_run(poe_batch *b, const int64_t *nsteps)
         BK(cudaStreamWaitEvent(ctx->stream, b->done, 0));
         for (ShotHost &s : ctx->shots) s.steps += nsteps[i];
     }
+    return POE_OK;
+}
+
+int poe_batch_tune_span(poe_batch *b, int32_t span)
+{
+    if (!b) return POE_EINVAL;
+    if (span != 0 && span != 1) return bfail(b, POE_EINVAL, "tuning: span must be 0 or 1");
+    if ((span != 0) != b->span) {
+        BK(cudaStreamSynchronize(b->stream));   // a graph still running holds the old launches
+        drop_batch_graphs(b);
+    }
+    b->span = span != 0;
     return POE_OK;
 }
 

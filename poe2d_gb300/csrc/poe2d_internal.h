@@ -53,7 +53,7 @@ struct ModelDev {
     const uint8_t *ids;      // padded plane of material ids (pitch P bytes, R rows), or null
     const float *mtab;       // nmat rows of MT_W floats
     int nmat;
-    int ntx;                 // tiles across x of the kernel this model runs on (receiver lists)
+    int ntx, ntz;            // tiles across x and z of the step kernel (receiver lists, tile flags)
     // TMA descriptors (device memory) of the id plane (palette models only) and
     // of the 6 x-profile and 6 z-profile rows, boxed for the step kernel's tiles
     const void *tm_ids, *tm_px, *tm_pz;
@@ -102,25 +102,31 @@ struct StreamShot {
     int64_t trace_cap;
     const void *tm_v;      // TMA descriptors over both state buffers (palette mode)
     const void *tm_s;
+    int *done;             // per tile (tz ntx + tx): a step it has completed (step-spanning launches);
+                           // never ahead of the shot (zeroed on reset and restore), the first step of a
+                           // launch waits for none, later steps only for flags published in the launch
 };
 
-// one step of a model's shots over the work list items[0..nitems) of
-// (0, shot, x0, z0)
+// nk steps (k .. k+nk-1 of the graph or run, n = *step + k + 1 ...) of a model's
+// shots over the work list items[0..nitems) of (0, shot, x0, z0).  nk = 1:
+// one launch per step.  nk > 1: one step-spanning launch, in which a tile of
+// step n > its first starts once its 3 x 3 neighbourhood has completed step
+// n-1 (the shots' done flags)
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     bool exact, bool kone, void *stream);
+                     int nk, bool exact, bool kone, void *stream);
 // one step over several models: items (model, shot, x0, z0) index models_dev and shots_dev;
 // exact_few: every model's spacings have a 24 h of few bits; coef: the models read
 // their 8 coefficient planes per cell (all of them), else each has a material palette
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool exact_few, bool coef, bool kone, void *stream);
+                      int nk, bool exact, bool exact_few, bool coef, bool kone, void *stream);
 // the step kernel of one stencil mode (poe2d_tile_fast.cu, poe2d_tile_exact.cu,
 // poe2d_tile_exact_any.cu): models null for a single model m, else a batch
 int tile_step_fast(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                   int k, bool kone, bool coef, void *stream);
+                   int k, int nk, bool kone, bool coef, void *stream);
 int tile_step_exact(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                    int k, bool kone, bool coef, void *stream);
+                    int k, int nk, bool kone, bool coef, void *stream);
 int tile_step_exact_any(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-                        int nitems, int k, bool kone, bool coef, void *stream);
+                        int nitems, int k, int nk, bool kone, bool coef, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
 // one thread waits, polls times at most, on an mbarrier no thread arrives at;

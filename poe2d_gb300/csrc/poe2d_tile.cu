@@ -1,7 +1,8 @@
-// poe2d_tile.cu -- launches of the fused step kernel (its variants are
-// compiled in poe2d_tile_fast.cu, poe2d_tile_exact.cu and
-// poe2d_tile_exact_any.cu from poe2d_tile.cuh) and the small kernels around
-// it: step clocks, the bounded-wait check, derived fields.
+// poe2d_tile.cu -- launches of the fused step kernel, one step per launch or
+// a step-spanning launch of several (its variants are compiled in
+// poe2d_tile_fast.cu, poe2d_tile_exact.cu and poe2d_tile_exact_any.cu from
+// poe2d_tile.cuh), and the small kernels around it: step clocks, the
+// bounded-wait check, derived fields.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -22,29 +23,29 @@ int stencil_mode(bool exact, bool few)
 }
 
 int step_mode(int sm, const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-              int nitems, int k, bool kone, bool coef, void *stream)
+              int nitems, int k, int nk, bool kone, bool coef, void *stream)
 {
     switch (sm) {
-    case SM_FAST: return tile_step_fast(m, models, shots, items, nitems, k, kone, coef, stream);
-    case SM_EXACT_FEW: return tile_step_exact(m, models, shots, items, nitems, k, kone, coef, stream);
-    default: return tile_step_exact_any(m, models, shots, items, nitems, k, kone, coef, stream);
+    case SM_FAST: return tile_step_fast(m, models, shots, items, nitems, k, nk, kone, coef, stream);
+    case SM_EXACT_FEW: return tile_step_exact(m, models, shots, items, nitems, k, nk, kone, coef, stream);
+    default: return tile_step_exact_any(m, models, shots, items, nitems, k, nk, kone, coef, stream);
     }
 }
 }  // namespace
 
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     bool exact, bool kone, void *stream)
+                     int nk, bool exact, bool kone, void *stream)
 {
     (void)nshots;
     return step_mode(stencil_mode(exact, m.qx.few_bits && m.qz.few_bits), m, nullptr, shots_dev, items, nitems, k,
-                     kone, m.ids == nullptr, stream);
+                     nk, kone, m.ids == nullptr, stream);
 }
 
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      bool exact, bool exact_few, bool coef, bool kone, void *stream)
+                      int nk, bool exact, bool exact_few, bool coef, bool kone, void *stream)
 {
     const ModelDev dummy{};
-    return step_mode(stencil_mode(exact, exact_few), dummy, models_dev, shots_dev, items, nitems, k, kone, coef,
+    return step_mode(stencil_mode(exact, exact_few), dummy, models_dev, shots_dev, items, nitems, k, nk, kone, coef,
                      stream);
 }
 

@@ -184,6 +184,41 @@ __device__ __forceinline__ float gld(const float *p) { return __ldca(p); }
 // stores since they cannot alias them
 __device__ __forceinline__ float gld_ro(const float *p) { return __ldg(p); }
 
+// Step-spanning launches (MS): the C-PML memory a tile reads was written by
+// other CTAs of the same launch at the previous step, so it is read through
+// L2 only (this SM's L1 could still hold a line of an older step) and
+// prefetched to L2; one launch per step reads it as above.
+template <bool MS>
+__device__ __forceinline__ float gld_m(const float *p)
+{
+    return MS ? __ldcg(p) : gld(p);
+}
+template <bool MS>
+__device__ __forceinline__ float gld_ro_m(const float *p)
+{
+    return MS ? __ldcg(p) : gld_ro(p);
+}
+template <bool MS>
+__device__ __forceinline__ void prefetch_m(const float *p)
+{
+    if (MS) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+    else asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+// a tile flag of a step-spanning launch: read with acquire, published with
+// release, both at GPU scope
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// orders generic-proxy global accesses against later async-proxy (TMA) ones
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
 // 330-353): co = (rho m - rhof^2)/dt, c1,2 = co +- rho (eta/kappa)/2
@@ -247,10 +282,20 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 
 }  // namespace tile
 
-template <int SM, bool KONE, bool MULTI, bool COEF>
+// MS (step-spanning launch): the launch runs steps k .. k+nk-1 and walks
+// (step, tile) items step by step: item g is tile g % nitems of step
+// k + g / nitems.  Before the producer fills a buffer with a tile of step n it
+// waits until the tile's 3 x 3 neighbourhood (the cells its boxes read, and
+// the readers of the buffer it will overwrite) has completed step n-1, by
+// the shots' done flags; it publishes its own tiles' flags once the compute
+// warps have released their buffers.  A CTA only ever waits for items of
+// earlier steps, which every CTA finishes before it moves on, so the waits
+// cannot close a cycle; the producer keeps publishing its own finished items
+// while it waits.  Without MS (nk = 1) no tile waits for another.
+template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
 __global__ void __launch_bounds__(tile::PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
-           const int4 *__restrict__ items, int nitems, int k, int prefetch)
+           const int4 *__restrict__ items, int nitems, int k, int nk, int prefetch)
 {
     using namespace tile;
     constexpr bool EXACT = SM != SM_FAST;
@@ -270,12 +315,33 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     }
     __syncthreads();
 
+    const int total = MS ? nk * nitems : nitems;   // items of this launch
     // ------------------------------------------------------------ producer
     if (tid >= PCT) {
         const int lane = tid - PCT;
+        // MS: the flag and step of the item in each buffer, published once its
+        // compute warps have released the buffer (lane 0's copy is the live one)
+        int *pend_flag[2] = {nullptr, nullptr};
+        int pend_n[2] = {0, 0};
+        // publish item i if its buffer has been released; true when nothing of
+        // item i is left to publish
+        auto publish = [&](int i) -> bool {
+            if (!MS || lane != 0 || i < 0 || !pend_flag[i & 1]) return true;
+            if (!mbar_try_wait(&empty[i & 1], (uint32_t)((i >> 1) & 1))) return false;
+            // the compute warps' global stores, ordered before their arrivals,
+            // become visible before the flag does (to generic and TMA readers)
+            __threadfence();
+            fence_proxy_async_global();
+            st_release(pend_flag[i & 1], pend_n[i & 1]);
+            pend_flag[i & 1] = nullptr;
+            return true;
+        };
         int j = 0;
-        for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
+        bool gave_up = false;
+        for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
             const int b = j & 1;
+            const int w = MS ? g % nitems : g;
+            const int kk = MS ? k + g / nitems : k;
             // Resolve the item (a chain of dependent global loads) while buffer b
             // is still being computed on, so the copies start the moment it frees.
             const int4 it = items[w];
@@ -286,8 +352,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             ItemMeta M;
             const void *tm_v = nullptr, *tm_s = nullptr;
             int cv = 0;
+            int64_t n = 0;
             if (lane == 0) {
-                const int64_t n = *S.step + k + 1;
+                n = *S.step + kk + 1;
                 const int rd = (int)((n - 1) & 1), wr = (int)(n & 1);
                 M.FB = S.f[wr];
                 M.mxr = S.mx[rd];
@@ -297,7 +364,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 M.mxv = S.mxv;
                 M.mzv = S.mzv;
                 M.acc_w = S.acc + wr;
-                M.pacc = S.acc[rd];
+                M.pacc = __ldcg(S.acc + rd);   // written at the previous step, maybe by another CTA
                 M.src_off = (int)S.src_off;
                 M.src_where = S.src_where;
                 M.src_on = n <= S.src_n;
@@ -338,12 +405,52 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 if (lane < MDW) md0 = msrc[lane];
                 if (lane + 32 < MDW) md1 = msrc[lane + 32];
             }
+            int *my_flag = nullptr;
+            if (MS) {
+                // the 3 x 3 neighbourhood of the tile must have completed step n-1:
+                // lane l < 9 watches the tile (tx + l % 3 - 1, tz + l / 3 - 1).  The
+                // launch's first step waits for none: the previous launch ended
+                // (the flags may lag behind the shot, never lead it).
+                const int nn = __shfl_sync(0xffffffffu, (int)n, 0);
+                const int tx = x0 / QX, tz = z0 / QZ, ntx = m.ntx, ntz = m.ntz;
+                const int ux = tx + lane % 3 - 1, uz = tz + lane / 3 - 1;
+                const int *flag = (kk > k && lane < 9 && ux >= 0 && ux < ntx && uz >= 0 && uz < ntz)
+                                      ? S.done + uz * ntx + ux
+                                      : nullptr;
+                my_flag = S.done + tz * ntx + tx;
+                bool ok = flag == nullptr;
+                for (int poll = 0;; ++poll) {
+                    if (!ok) ok = ld_acquire(flag) >= nn - 1;
+                    if (__all_sync(0xffffffffu, ok)) break;
+                    publish(j - 1);          // a neighbour may be this CTA's own item in flight
+                    publish(j - 2);
+                    if (poll >= (1 << 20)) {
+                        gave_up = true;
+                        break;
+                    }
+                }
+                if (gave_up) {
+                    if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
+                    break;
+                }
+                // lanes 1-8 acquired the flags, lane 0 issues the copies: the warp
+                // barrier and a GPU-scope fence order the one after the other
+                __syncwarp();
+                if (lane == 0 && kk > k) __threadfence();
+            }
             if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
-                if (lane == 0) atomicExch(mp.err ? mp.err : models[items[w].x].err, 1);
+                if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
+                gave_up = true;
                 break;
             }
+            publish(j - 2);                  // its buffer was just released
             unsigned char *buf = smp + b * BUF_BYTES;
             if (lane == 0) {
+                if (MS) {
+                    fence_proxy_async_global();   // the neighbours' stores, acquired above, before the copies
+                    pend_flag[b] = my_flag;
+                    pend_n[b] = (int)n;
+                }
                 // the big copies first: the 4 velocity planes with a 4-cell halo and
                 // the 5 state planes with a 2-row halo, one box each (bytes
                 // announced, no arrival yet)
@@ -376,6 +483,12 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         }
         // copies in flight land before the CTA may exit: the last two fills
         for (int i = j - 2 < 0 ? 0 : j - 2; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
+        // MS: the last items' flags, once their compute is done (bounded; a
+        // compute wait that gave up flags the error itself)
+        if (MS && !gave_up)
+            for (int i = j - 2; i < j; ++i)
+                for (int poll = 0; poll < (1 << 20) && !publish(i); ++poll) {
+                }
         return;
     }
 
@@ -391,7 +504,8 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         compute_sync();
     }
     int j = 0;
-    for (int w = blockIdx.x; w < nitems; w += gridDim.x, ++j) {
+    for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
+        const int w = MS ? g % nitems : g;
         const int b = j & 1;
         unsigned char *buf = smp + b * BUF_BYTES;
         // No barrier here: warps run ahead into the item as soon as its data
@@ -457,11 +571,11 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (xc >= 0)
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxv + a * nzx + tz * Wx + xc));
+                            prefetch_m<MS>(IM.mxv + a * nzx + tz * Wx + xc);
                     if (zr >= 0)
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzv + a * hzp + zr * P + x + XH));
+                            prefetch_m<MS>(IM.mzv + a * hzp + zr * P + x + XH);
                 }
             };
             if (MULTI) prefetch_velocity_memory();
@@ -488,11 +602,11 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (xc >= 0)
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mxr + a * nzx + z * Wx + xc));
+                            prefetch_m<MS>(IM.mxr + a * nzx + z * Wx + xc);
                     if (zr >= 0)
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
-                            asm volatile("prefetch.global.L1 [%0];" ::"l"(IM.mzr + a * hzp + zr * P + x + XH));
+                            prefetch_m<MS>(IM.mzr + a * hzp + zr * P + x + XH);
                 }
             }
             // ---- stress on the tile + 2-cell halo: column lx, rows zb0 .. zb0+3
@@ -567,9 +681,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (xc >= 0 && (g1 || g2)) {
                         const int ix = z * Wx + xc;
                         const float *MA = IM.mxr;
-                        m1 = bxh * gld_ro(MA + MXS_SXX * nzx + ix) + axh * vdx;
-                        m3 = bxh * gld_ro(MA + MXS_S2 * nzx + ix) + axh * wdx;
-                        m5 = bx * gld_ro(MA + MXS_SXZ * nzx + ix) + ax * sdx;
+                        m1 = bxh * gld_ro_m<MS>(MA + MXS_SXX * nzx + ix) + axh * vdx;
+                        m3 = bxh * gld_ro_m<MS>(MA + MXS_S2 * nzx + ix) + axh * wdx;
+                        m5 = bx * gld_ro_m<MS>(MA + MXS_SXZ * nzx + ix) + ax * sdx;
                         if (own) {
                             float *MB = IM.mxw;
                             if (g1) {
@@ -583,9 +697,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         const int iz = zr * P + xi;
                         const float *MA = IM.mzr;
                         const float bz = PZs[PB * PZH + pzo], az = PZs[PA * PZH + pzo];
-                        m2 = bz * gld_ro(MA + MZS_SXX * hzp + iz) + az * vdz;
-                        m4 = bz * gld_ro(MA + MZS_S2 * hzp + iz) + az * wdz;
-                        m6 = PZs[PBH * PZH + pzo] * gld_ro(MA + MZS_SXZ * hzp + iz) + PZs[PAH * PZH + pzo] * sdz;
+                        m2 = bz * gld_ro_m<MS>(MA + MZS_SXX * hzp + iz) + az * vdz;
+                        m4 = bz * gld_ro_m<MS>(MA + MZS_S2 * hzp + iz) + az * wdz;
+                        m6 = PZs[PBH * PZH + pzo] * gld_ro_m<MS>(MA + MZS_SXZ * hzp + iz) + PZs[PAH * PZH + pzo] * sdz;
                         if (own) {
                             float *MB = IM.mzw;
                             if (g1) {
@@ -700,9 +814,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         const int ix = tz * Wx + xc;
                         float *M1 = MXV + MXV_VX1 * nzx + ix, *M2 = MXV + MXV_VX2 * nzx + ix;
                         float *M4 = MXV + MXV_VZ * nzx + ix;
-                        m1 = bx * gld(M1) + ax * d1x;
-                        m2 = bx * gld(M2) + ax * d2x;
-                        m4 = bxh * gld(M4) + axh * d1z;
+                        m1 = bx * gld_m<MS>(M1) + ax * d1x;
+                        m2 = bx * gld_m<MS>(M2) + ax * d2x;
+                        m4 = bxh * gld_m<MS>(M4) + axh * d1z;
                         if (gvx) {
                             gst(M1, m1);
                             gst(M2, m2);
@@ -714,9 +828,9 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                         float *M3 = MZV + MZV_VX * hzp + iz, *M5 = MZV + MZV_VZ1 * hzp + iz;
                         float *M6 = MZV + MZV_VZ2 * hzp + iz;
                         const float bh = PZs[PBH * PZH + pzo], ah = PZs[PAH * PZH + pzo];
-                        m3 = PZs[PB * PZH + pzo] * gld(M3) + PZs[PA * PZH + pzo] * d3x;
-                        m5 = bh * gld(M5) + ah * d2z;
-                        m6 = bh * gld(M6) + ah * d3z;
+                        m3 = PZs[PB * PZH + pzo] * gld_m<MS>(M3) + PZs[PA * PZH + pzo] * d3x;
+                        m5 = bh * gld_m<MS>(M5) + ah * d2z;
+                        m6 = bh * gld_m<MS>(M6) + ah * d3z;
                         if (gvx) gst(M3, m3);
                         if (gvz) {
                             gst(M5, m5);
@@ -800,35 +914,51 @@ inline int prefetch_strips(int nitems) { return nitems >= 8 * sm_count() ? 1 : 0
 
 // one launch of the step kernel of stencil mode SM: a single model (models
 // null) or a batch (models: device array; m unused)
-template <int SM, bool KONE, bool MULTI, bool COEF>
+template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
 int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                int k, cudaStream_t st)
+                int k, int nk, cudaStream_t st)
 {
     static std::atomic<uint64_t> done{0};
-    auto kern = k_tile_pal<SM, KONE, MULTI, COEF>;
+    auto kern = k_tile_pal<SM, KONE, MULTI, COEF, MS>;
     smem_attr_once(kern, (int)tile::PAL_SMEM, done);
     const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
-    if (grid > 0) kern<<<grid, tile::PNT, tile::PAL_SMEM, st>>>(m, models, shots, items, nitems, k,
-                                                                prefetch_strips(nitems));
-    return (int)cudaGetLastError();
+    if (grid <= 0) return (int)cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(tile::PNT);
+    cfg.dynamicSmemBytes = tile::PAL_SMEM;
+    cfg.stream = st;
+    // a step-spanning launch's CTAs wait for one another's tiles: a
+    // cooperative launch guarantees that all of them are resident at once
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = MS ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return (int)cudaLaunchKernelEx(&cfg, kern, m, models, shots, items, nitems, k, MS ? nk : 1,
+                                   prefetch_strips(nitems));
 }
 
-// every (KONE, MULTI, COEF) variant of one stencil mode
+// every (KONE, MULTI, COEF, step-spanning) variant of one stencil mode
 template <int SM>
 int tile_launch_mode(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-                     int nitems, int k, bool kone, bool coef, cudaStream_t st)
+                     int nitems, int k, int nk, bool kone, bool coef, cudaStream_t st)
 {
     const bool multi = models != nullptr;
-    switch ((kone ? 4 : 0) | (multi ? 2 : 0) | (coef ? 1 : 0)) {
-    case 0: return tile_launch<SM, false, false, false>(m, models, shots, items, nitems, k, st);
-    case 1: return tile_launch<SM, false, false, true>(m, models, shots, items, nitems, k, st);
-    case 2: return tile_launch<SM, false, true, false>(m, models, shots, items, nitems, k, st);
-    case 3: return tile_launch<SM, false, true, true>(m, models, shots, items, nitems, k, st);
-    case 4: return tile_launch<SM, true, false, false>(m, models, shots, items, nitems, k, st);
-    case 5: return tile_launch<SM, true, false, true>(m, models, shots, items, nitems, k, st);
-    case 6: return tile_launch<SM, true, true, false>(m, models, shots, items, nitems, k, st);
-    default: return tile_launch<SM, true, true, true>(m, models, shots, items, nitems, k, st);
+    switch ((kone ? 8 : 0) | (multi ? 4 : 0) | (coef ? 2 : 0) | (nk > 1 ? 1 : 0)) {
+#define POE_TILE_CASE(s, KO, MU, CO, MS) \
+    case s: return tile_launch<SM, KO, MU, CO, MS>(m, models, shots, items, nitems, k, nk, st);
+        POE_TILE_CASE(0, false, false, false, false) POE_TILE_CASE(1, false, false, false, true)
+        POE_TILE_CASE(2, false, false, true, false) POE_TILE_CASE(3, false, false, true, true)
+        POE_TILE_CASE(4, false, true, false, false) POE_TILE_CASE(5, false, true, false, true)
+        POE_TILE_CASE(6, false, true, true, false) POE_TILE_CASE(7, false, true, true, true)
+        POE_TILE_CASE(8, true, false, false, false) POE_TILE_CASE(9, true, false, false, true)
+        POE_TILE_CASE(10, true, false, true, false) POE_TILE_CASE(11, true, false, true, true)
+        POE_TILE_CASE(12, true, true, false, false) POE_TILE_CASE(13, true, true, false, true)
+        POE_TILE_CASE(14, true, true, true, false) POE_TILE_CASE(15, true, true, true, true)
+#undef POE_TILE_CASE
     }
+    return (int)cudaErrorInvalidValue;
 }
 
 }  // namespace poe

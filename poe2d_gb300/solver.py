@@ -237,9 +237,15 @@ class Solver:
         dealt for an even share of edge tiles per CTA) and graph length."""
         self._check(L.lib().poe_tune(self.h, int(order), int(graph_steps)))
 
+    def tune_span(self, span=1):
+        """1: one step-spanning launch per captured graph (tiles of a step start as
+        soon as their neighbourhood finished the previous one); 0: a launch per step."""
+        self._check(L.lib().poe_tune_span(self.h, int(span)))
+
     def autotune(self, trial_steps=128):
-        """Time the 8 (order, graph_steps) candidates, keep the fastest; shots must be
-        at step 0 and are reset after.  Returns (order, graph_steps, ms per candidate)."""
+        """Time the 16 (order, graph_steps, span) candidates, keep the fastest; shots must
+        be at step 0 and are reset after.  Returns (order, graph_steps, ms per candidate),
+        candidate c = order c // 4, graph_steps (16, 64)[(c // 2) % 2], span c % 2."""
         o, g = C.c_int32(0), C.c_int32(0)
         ms = np.zeros(L.AUTOTUNE_CANDIDATES, np.float32)
         self._check(L.lib().poe_autotune(self.h, int(trial_steps), C.byref(o), C.byref(g), _f(ms)))
@@ -321,6 +327,11 @@ class Batch:
     def sync(self):
         self._live()
         self._check(L.lib().poe_batch_sync(self.h))
+
+    def tune_span(self, span=1):
+        """Step-spanning launches for the batch (see Solver.tune_span)."""
+        self._live()
+        self._check(L.lib().poe_batch_tune_span(self.h, int(span)))
 
     @property
     def launches(self):

@@ -1,6 +1,7 @@
-"""The autotuner times the work-list orders and graph lengths on the context
-itself, keeps the fastest, and leaves the shots at step 0; whatever it picks,
-the results equal the default configuration's bit for bit."""
+"""The autotuner times the work-list orders, graph lengths and step-spanning
+launches on the context itself, keeps the fastest, and leaves the shots at
+step 0; whatever it picks, the results equal the default configuration's bit
+for bit."""
 import numpy as np
 import pytest
 
@@ -32,7 +33,9 @@ def _run(poe, m, tune):
             picked = s.autotune(32)
             assert all(s.steps(k) == 0 for k in range(len(srcs)))
         elif tune is not None:
-            s.tune(*tune)
+            s.tune(*tune[:2])
+            if len(tune) > 2:
+                s.tune_span(tune[2])
         s.run(150)
         return [s.traces(k) for k in range(len(srcs))] + [s.field("vz", 2)], picked
 
@@ -41,11 +44,11 @@ def test_autotune_keeps_results_and_reports_timings(poe):
     m = _model(poe)
     ref, _ = _run(poe, m, None)
     got, (order, gsteps, ms) = _run(poe, m, "auto")
-    assert order in (0, 1, 2, 3) and gsteps in (16, 64) and ms.shape == (8,)
-    assert np.all(ms > 0) and ms.argmin() == 2 * order + (1 if gsteps == 64 else 0)
+    assert order in (0, 1, 2, 3) and gsteps in (16, 64) and ms.shape == (16,)
+    assert np.all(ms > 0) and ms.argmin() // 2 == 2 * order + (1 if gsteps == 64 else 0)
     for a, b in zip(ref, got):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
-    for tune in ((1, 16), (2, 64), (3, 64), (3, 16)):
+    for tune in ((1, 16, 0), (2, 64, 1), (3, 64, 0), (3, 16, 1), (0, 64, 0)):
         other, _ = _run(poe, m, tune)
         for a, b in zip(ref, other):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
@@ -59,6 +62,8 @@ def test_tuning_arguments_are_checked(poe):
             s.tune(4, 64)
         with pytest.raises(poe.PoeError):
             s.tune(0, 0)
+        with pytest.raises(poe.PoeError):
+            s.tune_span(2)
         s.run(5)
         with pytest.raises(poe.PoeError):
             s.autotune(8)                     # shots not at step 0

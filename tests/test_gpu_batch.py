@@ -63,10 +63,15 @@ def _same(a, b):
 
 @pytest.mark.parametrize("palette", [True, False])
 @pytest.mark.parametrize("fast", [False, True])
-def test_batch_matches_single_runs(poe, fast, palette):
+@pytest.mark.parametrize("span", [1, 0])
+def test_batch_matches_single_runs(poe, fast, palette, span):
+    """The batch with step-spanning launches (span 1) or one launch per step
+    (span 0) against single runs with the other setting."""
     cases = _build(poe, fast)
     runs = [[150, 70, 0, 213, 64], [40, 0, 100, 64, 1]]     # uneven, with idle models and graph + tail segments
     ref = [_solver(poe, c, fast, palette) for c in cases]
+    for s in ref:
+        s.tune_span(1 - span)
     for r in runs:
         for i, s in enumerate(ref):
             if r[i]:
@@ -77,6 +82,7 @@ def test_batch_matches_single_runs(poe, fast, palette):
 
     solvers = [_solver(poe, c, fast, palette) for c in cases]
     with poe.Batch(solvers) as b:
+        b.tune_span(span)
         for r in runs:
             b.run(r)
         b.sync()
@@ -133,3 +139,30 @@ def test_batch_at_a_spacing_whose_24h_has_many_bits(poe):
         _same(_state(s, 1), w)
     for s in ref + solvers:
         s.close()
+
+
+@pytest.mark.parametrize("fast", [False, True])
+@pytest.mark.parametrize("palette", [True, False])
+def test_step_spanning_launches_equal_one_launch_per_step(poe, fast, palette):
+    """One context with several shots: step-spanning launches (a tile of step
+    n starts once its neighbourhood has finished step n-1) end exactly where
+    one launch per step ends, through graphs (64 steps), the direct tail, a
+    single step, a reset and a restored checkpoint."""
+    case = _build(poe, fast)[1][:4] + ([poe.source(60, 20, poe.SRC_RICKER_FZ, 250.0, 1e3, 0.0),
+                                       poe.source(190, 40, poe.SRC_REF_DGAUSS_P, 250.0, 1.0, 0.4)],
+                                      _build(poe, fast)[1][5])
+    out = []
+    for span in (0, 1):
+        s = _solver(poe, case, fast, palette)
+        s.tune_span(span)
+        s.run(150)                         # two 64-step graphs and a 22-step direct launch
+        s.run(1)
+        img = s.checkpoint(1)
+        s.run(63)
+        s.reset_shot(0)
+        s.run(70)                          # shot 0 from step 0 again, shot 1 on from 214
+        s.restore(img, 1)                  # shot 1 back to step 151 (its tile flags go back too)
+        s.run(40)
+        out.append(_state(s, 2))
+        s.close()
+    _same(out[0], out[1])
