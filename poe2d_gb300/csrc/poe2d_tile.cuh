@@ -293,7 +293,7 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 // cannot close a cycle; the producer keeps publishing its own finished items
 // while it waits.  Without MS (nk = 1) no tile waits for another.
 template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
-__global__ void __launch_bounds__(tile::PNT, 1)
+__global__ void __launch_bounds__(MS ? tile::PNT + 32 : tile::PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
            const int4 *__restrict__ items, int nitems, int k, int nk, int prefetch)
 {
@@ -304,38 +304,56 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     uint64_t *empty = full + 2;
+    uint64_t *pub = full + 4;                  // MS: an item's flag published (publisher -> producer)
     const int tid = threadIdx.x;
 
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
             mbar_init(&full[b], 1);
             mbar_init(&empty[b], NW);
+            mbar_init(&pub[b], 1);
         }
         mbar_fence_init();
     }
     __syncthreads();
 
     const int total = MS ? nk * nitems : nitems;   // items of this launch
+
+    // ------------------------------------------------------------ publisher (MS)
+    // Publishes each item's tile flag once the compute warps have released its
+    // buffer, then lets the producer reuse the buffer: a warp of its own, so
+    // neither the producer's copies nor its waits for other tiles hold it up.
+    if (MS && tid >= PCT + 32) {
+        int j = 0;
+        for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
+            const int b = j & 1;
+            int *flag = nullptr;
+            int nval = 0;
+            if (tid == PCT + 32) {
+                const int4 it = items[g % nitems];
+                const ModelDev &m = MULTI ? models[it.x] : mp;
+                const StreamShot &S = shots[it.y];
+                flag = S.done + (it.w / QZ) * m.ntx + it.z / QX;
+                nval = (int)(*S.step + k + g / nitems + 1);
+            }
+            if (!mbar_wait(&empty[b], (uint32_t)((j >> 1) & 1))) {
+                if (tid == PCT + 32) atomicExch(mp.err ? mp.err : models[items[g % nitems].x].err, 1);
+                return;
+            }
+            if (tid == PCT + 32) {
+                // the compute warps' global stores, ordered before their arrivals,
+                // are released with the flag (to generic and TMA readers)
+                fence_proxy_async_global();
+                st_release(flag, nval);
+                mbar_arrive(&pub[b]);
+            }
+            __syncwarp();
+        }
+        return;
+    }
     // ------------------------------------------------------------ producer
-    if (tid >= PCT) {
+    if (tid >= PCT) {   // (the warp after the compute warps)
         const int lane = tid - PCT;
-        // MS: the flag and step of the item in each buffer, published once its
-        // compute warps have released the buffer (lane 0's copy is the live one)
-        int *pend_flag[2] = {nullptr, nullptr};
-        int pend_n[2] = {0, 0};
-        // publish item i if its buffer has been released; true when nothing of
-        // item i is left to publish
-        auto publish = [&](int i) -> bool {
-            if (!MS || lane != 0 || i < 0 || !pend_flag[i & 1]) return true;
-            if (!mbar_try_wait(&empty[i & 1], (uint32_t)((i >> 1) & 1))) return false;
-            // the compute warps' global stores, ordered before their arrivals,
-            // become visible before the flag does (to generic and TMA readers)
-            __threadfence();
-            fence_proxy_async_global();
-            st_release(pend_flag[i & 1], pend_n[i & 1]);
-            pend_flag[i & 1] = nullptr;
-            return true;
-        };
         int j = 0;
         bool gave_up = false;
         for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
@@ -405,7 +423,6 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 if (lane < MDW) md0 = msrc[lane];
                 if (lane + 32 < MDW) md1 = msrc[lane + 32];
             }
-            int *my_flag = nullptr;
             if (MS) {
                 // the 3 x 3 neighbourhood of the tile must have completed step n-1:
                 // lane l < 9 watches the tile (tx + l % 3 - 1, tz + l / 3 - 1).  The
@@ -417,13 +434,10 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 const int *flag = (kk > k && lane < 9 && ux >= 0 && ux < ntx && uz >= 0 && uz < ntz)
                                       ? S.done + uz * ntx + ux
                                       : nullptr;
-                my_flag = S.done + tz * ntx + tx;
                 bool ok = flag == nullptr;
                 for (int poll = 0;; ++poll) {
                     if (!ok) ok = ld_acquire(flag) >= nn - 1;
                     if (__all_sync(0xffffffffu, ok)) break;
-                    publish(j - 1);          // a neighbour may be this CTA's own item in flight
-                    publish(j - 2);
                     if (poll >= (1 << 20)) {
                         gave_up = true;
                         break;
@@ -433,24 +447,20 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
                     break;
                 }
-                // lanes 1-8 acquired the flags, lane 0 issues the copies: the warp
-                // barrier and a GPU-scope fence order the one after the other
+                // lanes 0-8 acquired the flags, lane 0 issues the copies: the warp
+                // barrier orders the one after the other
                 __syncwarp();
-                if (lane == 0 && kk > k) __threadfence();
             }
-            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
+            // buffer b free again: released by the compute warps (and, MS, its
+            // item's flag published)
+            if (j >= 2 && !mbar_wait(MS ? &pub[b] : &empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
                 if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
                 gave_up = true;
                 break;
             }
-            publish(j - 2);                  // its buffer was just released
             unsigned char *buf = smp + b * BUF_BYTES;
             if (lane == 0) {
-                if (MS) {
-                    fence_proxy_async_global();   // the neighbours' stores, acquired above, before the copies
-                    pend_flag[b] = my_flag;
-                    pend_n[b] = (int)n;
-                }
+                if (MS) fence_proxy_async_global();   // the neighbours' stores, acquired above, before the copies
                 // the big copies first: the 4 velocity planes with a 4-cell halo and
                 // the 5 state planes with a 2-row halo, one box each (bytes
                 // announced, no arrival yet)
@@ -483,12 +493,6 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         }
         // copies in flight land before the CTA may exit: the last two fills
         for (int i = j - 2 < 0 ? 0 : j - 2; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
-        // MS: the last items' flags, once their compute is done (bounded; a
-        // compute wait that gave up flags the error itself)
-        if (MS && !gave_up)
-            for (int i = j - 2; i < j; ++i)
-                for (int poll = 0; poll < (1 << 20) && !publish(i); ++poll) {
-                }
         return;
     }
 
@@ -925,7 +929,7 @@ int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *sho
     if (grid <= 0) return (int)cudaGetLastError();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(tile::PNT);
+    cfg.blockDim = dim3(MS ? tile::PNT + 32 : tile::PNT);   // MS: + the publisher warp
     cfg.dynamicSmemBytes = tile::PAL_SMEM;
     cfg.stream = st;
     // a step-spanning launch's CTAs wait for one another's tiles: a
