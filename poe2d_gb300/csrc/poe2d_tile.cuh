@@ -218,6 +218,17 @@ __device__ __forceinline__ void st_release(int *p, int v)
 }
 // orders generic-proxy global accesses against later async-proxy (TMA) ones
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+// a CTA-scope counter in shared memory: added to with release, read with acquire
+__device__ __forceinline__ void red_add_release_cta(int *p, int v)
+{
+    asm volatile("red.release.cta.shared::cta.add.s32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire_cta(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
 
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
@@ -304,14 +315,16 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     extern __shared__ __align__(128) unsigned char smp[];
     uint64_t *full = reinterpret_cast<uint64_t *>(smp + PAL_OFF_B);
     uint64_t *empty = full + 2;
-    uint64_t *pub = full + 4;                  // MS: an item's flag published (publisher -> producer)
+    // MS: compute-warp releases of each buffer, counted (monotonic, so the
+    // publisher may lag behind the buffer's reuse without losing count)
+    int *released = reinterpret_cast<int *>(full + 4);
     const int tid = threadIdx.x;
 
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
             mbar_init(&full[b], 1);
             mbar_init(&empty[b], NW);
-            mbar_init(&pub[b], 1);
+            released[b] = 0;
         }
         mbar_fence_init();
     }
@@ -320,37 +333,35 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     const int total = MS ? nk * nitems : nitems;   // items of this launch
 
     // ------------------------------------------------------------ publisher (MS)
-    // Publishes each item's tile flag once the compute warps have released its
-    // buffer, then lets the producer reuse the buffer: a warp of its own, so
-    // neither the producer's copies nor its waits for other tiles hold it up.
+    // Publishes each item's tile flag once all compute warps have released its
+    // buffer: a warp of its own, off the path from a buffer's release to its
+    // refill, so neither the producer's copies nor its waits for other tiles
+    // hold it up, and it holds up neither.
     if (MS && tid >= PCT + 32) {
+        if (tid != PCT + 32) return;
         int j = 0;
         for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
             const int b = j & 1;
-            int *flag = nullptr;
-            int nval = 0;
-            if (tid == PCT + 32) {
-                const int4 it = items[g % nitems];
-                const ModelDev &m = MULTI ? models[it.x] : mp;
-                const StreamShot &S = shots[it.y];
-                flag = S.done + (it.w / QZ) * m.ntx + it.z / QX;
-                nval = (int)(*S.step + k + g / nitems + 1);
-            }
-            if (!mbar_wait(&empty[b], (uint32_t)((j >> 1) & 1))) {
-                if (tid == PCT + 32) atomicExch(mp.err ? mp.err : models[items[g % nitems].x].err, 1);
-                return;
-            }
-            if (tid == PCT + 32) {
-                // the compute warps' global stores, ordered before their arrivals,
-                // are released with the flag (to generic and TMA readers)
-                fence_proxy_async_global();
-                st_release(flag, nval);
-                mbar_arrive(&pub[b]);
-            }
-            __syncwarp();
+            const int4 it = items[g % nitems];
+            const ModelDev &m = MULTI ? models[it.x] : mp;
+            const StreamShot &S = shots[it.y];
+            int *flag = S.done + (it.w / QZ) * m.ntx + it.z / QX;
+            const int nval = (int)(*S.step + k + g / nitems + 1);
+            const int want = NW * ((j >> 1) + 1);   // releases of buffer b once item j is done
+            int poll = 0;
+            while (ld_acquire_cta(&released[b]) < want)
+                if (++poll > (1 << 22)) {
+                    atomicExch(mp.err ? mp.err : models[it.x].err, 1);
+                    return;
+                }
+            // the compute warps' global stores, acquired through the counter, are
+            // released with the flag (to generic and TMA readers)
+            fence_proxy_async_global();
+            st_release(flag, nval);
         }
         return;
     }
+
     // ------------------------------------------------------------ producer
     if (tid >= PCT) {   // (the warp after the compute warps)
         const int lane = tid - PCT;
@@ -451,9 +462,8 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 // barrier orders the one after the other
                 __syncwarp();
             }
-            // buffer b free again: released by the compute warps (and, MS, its
-            // item's flag published)
-            if (j >= 2 && !mbar_wait(MS ? &pub[b] : &empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
+            // buffer b free again: released by the compute warps
+            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
                 if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
                 gave_up = true;
                 break;
@@ -888,10 +898,14 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
             return;
         }
-        // hand buffer b back to the producer
+        // hand buffer b back to the producer (and, MS, count the release for the
+        // publisher; the warp barrier orders every lane's stores before both)
         fence_proxy_async();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[b]);
+        if (lane == 0) {
+            if (MS) red_add_release_cta(&released[b], 1);
+            mbar_arrive(&empty[b]);
+        }
     }
 }
 
