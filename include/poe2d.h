@@ -295,16 +295,19 @@ enum {
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 
-/* Step-spanning launches (no reference counterpart): span = 1 (the
- * default) runs the graph_steps steps of each captured graph as ONE
- * persistent launch, in which a tile of step n starts as soon as its 3 x 3
- * neighbourhood of tiles has completed step n-1 (per-tile flags in device
- * memory, bounded waits), so the steps overlap instead of each ending on its
- * slowest CTA; span = 0 launches the step kernel once per step.  Results do
- * not depend on it. */
+/* Step-spanning launches (no reference counterpart).  POE_SPAN_ALWAYS runs
+ * the graph_steps steps of each captured graph as ONE persistent launch, in
+ * which a tile of step n starts as soon as its 3 x 3 neighbourhood of tiles
+ * has completed step n-1 (per-tile flags in device memory, bounded waits), so
+ * the steps overlap instead of each ending on its slowest CTA;
+ * POE_SPAN_NEVER launches the step kernel once per step; POE_SPAN_AUTO (the
+ * default) spans when a step holds at most 24 tiles per SM (one 2001 x 2001
+ * shot: 14), where the step tail it removes is a large share of the step.
+ * Results do not depend on it. */
+enum { POE_SPAN_NEVER = 0, POE_SPAN_ALWAYS = 1, POE_SPAN_AUTO = 2 };
 int poe_tune_span(poe_ctx *ctx, int32_t span);
 
-/* Time every (order, graph_steps in {16, 64}, span in {0, 1}) candidate on
+/* Time every (order, graph_steps in {16, 64}, span NEVER or ALWAYS) candidate on
  * this context for trial_steps steps, keep the fastest and report it;
  * ms_out (may be NULL) receives the POE_AUTOTUNE_CANDIDATES timings,
  * candidate c = order c / 4, graph_steps {16, 64}[(c / 2) % 2], span c % 2.

@@ -20,6 +20,7 @@ CTX_NO_PALETTE = 2
 MAX_MATERIALS, MROW = 64, 14
 ORDER_ROWS, ORDER_COLUMNS, ORDER_TILE_MAJOR, ORDER_BALANCED = range(4)
 AUTOTUNE_CANDIDATES = 16
+SPAN_NEVER, SPAN_ALWAYS, SPAN_AUTO = range(3)
 M_CO, M_C1, M_C2, M_RHOF_EOK, M_RCO, M_RC1 = range(8, 14)
 FIELDS = ["vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22", "xi1", "xi2"]
 COEFS = ["rho", "rhof", "rsm", "eok", "lambdac", "mu", "alpha", "rbm"]

@@ -26,6 +26,11 @@ using namespace poe;
 
 namespace {
 constexpr int kGraphSteps = 64;
+// POE_SPAN_AUTO: step-spanning launches for steps of at most this many tiles
+// per SM (measured: a 2001^2 shot, 14 per SM, +13 %; one 1001^2 shot, 3.6, +29 %;
+// 16 shots of 1001^2, 57 per SM, -11 %: with many tiles per step the step tail
+// the spanning removes is small and its per-tile costs remain)
+constexpr int kSpanTilesPerSM = 24;
 }
 
 struct ShotHost {
@@ -79,7 +84,7 @@ struct poe_ctx {
     int ntx = 1, ntz = 1;       // tiles across x and z
     int order = POE_ORDER_BALANCED;   // work-list order (POE_ORDER_*)
     int graph_steps = kGraphSteps;   // steps per captured graph
-    bool span = true;                // a step-spanning launch per graph (else one launch per step)
+    int span = POE_SPAN_AUTO;        // step-spanning launches (POE_SPAN_*)
     int tile_x = PAL_TX, tile_z = PAL_TZ;
     poe_batch *batch = nullptr;   // the batch this context belongs to, if any
     uint64_t prof_hash = 0;       // of the C-PML profiles given to poe_create
@@ -363,7 +368,10 @@ int step_launch(poe_ctx *ctx, int k, int nk)
 // per step); returns the launches issued, or -1 with ctx->err set
 int64_t issue_steps(poe_ctx *ctx, int64_t nsteps)
 {
-    if (ctx->span && nsteps > 1) {
+    const bool span = ctx->span == POE_SPAN_ALWAYS ||
+                      (ctx->span == POE_SPAN_AUTO &&
+                       (int64_t)ctx->items.size() <= (int64_t)kSpanTilesPerSM * device_sms(ctx->device));
+    if (span && nsteps > 1) {
         const int r = step_launch(ctx, 0, (int)nsteps);
         if (r) return fail(ctx, POE_ECUDA, std::string("kernel launch: ") + cudaGetErrorString((cudaError_t)r)), -1;
         return 1;
@@ -1152,9 +1160,10 @@ int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps)
 int poe_tune_span(poe_ctx *ctx, int32_t span)
 {
     if (!ctx) return POE_EINVAL;
-    if (span != 0 && span != 1) return fail(ctx, POE_EINVAL, "tuning: span must be 0 or 1");
-    if ((span != 0) != ctx->span) drop_graph(ctx);
-    ctx->span = span != 0;
+    if (span != POE_SPAN_NEVER && span != POE_SPAN_ALWAYS && span != POE_SPAN_AUTO)
+        return fail(ctx, POE_EINVAL, "tuning: span must be POE_SPAN_NEVER, POE_SPAN_ALWAYS or POE_SPAN_AUTO");
+    if (span != ctx->span) drop_graph(ctx);
+    ctx->span = span;
     return POE_OK;
 }
 
@@ -1273,13 +1282,14 @@ struct poe_batch {
     int device = 0;
     bool exact = true, kone = true, few = true;
     bool coef = false;          // the models read their coefficient planes per cell
-    bool span = true;           // a step-spanning launch per graph (else one launch per step)
+    int span = POE_SPAN_AUTO;   // step-spanning launches (POE_SPAN_*)
     ModelDev *models_dev = nullptr;
     StreamShot *shots_dev = nullptr;
     int4 *items_dev = nullptr;
     int models_cap = 0, shots_cap = 0, items_cap = 0;
     std::vector<std::array<int, 2>> graph_keys;   // (items, shots) prefix of each graph
     std::vector<cudaGraphExec_t> graphs;
+    std::vector<int64_t> graph_kernels;            // kernels one walk of each graph launches
     cudaEvent_t done = nullptr;
     int64_t launches = 0;
     bool orphaned = false;      // a member context was destroyed: the batch no longer runs
@@ -1314,6 +1324,7 @@ void drop_batch_graphs(poe_batch *b)
     for (cudaGraphExec_t g : b->graphs) cudaGraphExecDestroy(g);
     b->graphs.clear();
     b->graph_keys.clear();
+    b->graph_kernels.clear();
 }
 
 template <class T>
@@ -1334,7 +1345,8 @@ int grow(poe_batch *b, T **p, int &cap, int need)
 // step-spanning launch, or one per step); returns the launches or -1
 int64_t batch_issue(poe_batch *b, int nitems, int64_t nsteps)
 {
-    const bool span = b->span && nsteps > 1;
+    const bool span = nsteps > 1 && (b->span == POE_SPAN_ALWAYS ||
+                                     (b->span == POE_SPAN_AUTO && nitems <= kSpanTilesPerSM * device_sms(b->device)));
     const int64_t nl = span ? 1 : nsteps;
     for (int64_t k = 0; k < nl; ++k) {
         const int r = launch_batch_step(b->models_dev, b->shots_dev, b->items_dev, nitems, (int)k,
@@ -1354,13 +1366,19 @@ int batch_steps(poe_batch *b, int nitems, int nshots, int64_t nsteps)
     return POE_OK;
 }
 
-cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
+// the graph of kGraphSteps steps over the first nitems items, captured on
+// first use; *kernels = the kernels one walk of it launches
+cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots, int64_t *kernels)
 {
     for (size_t i = 0; i < b->graph_keys.size(); ++i)
-        if (b->graph_keys[i][0] == nitems && b->graph_keys[i][1] == nshots) return b->graphs[i];
+        if (b->graph_keys[i][0] == nitems && b->graph_keys[i][1] == nshots) {
+            *kernels = b->graph_kernels[i];
+            return b->graphs[i];
+        }
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
-    int rc = batch_issue(b, nitems, kGraphSteps) < 0 ? 1 : 0;
+    const int64_t l = batch_issue(b, nitems, kGraphSteps);
+    int rc = l < 0 ? 1 : 0;
     if (rc == 0) rc = launch_advance_shots(b->shots_dev, nshots, kGraphSteps, b->stream);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc != 0 || e != cudaSuccess) {
@@ -1373,6 +1391,8 @@ cudaGraphExec_t batch_graph(poe_batch *b, int nitems, int nshots)
     if (ei != cudaSuccess) return nullptr;
     b->graph_keys.push_back({nitems, nshots});
     b->graphs.push_back(x);
+    b->graph_kernels.push_back(l + 1);
+    *kernels = l + 1;
     return x;
 }
 
@@ -1380,11 +1400,12 @@ int batch_segment(poe_batch *b, int nitems, int nshots, int64_t nsteps)
 {
     int64_t left = nsteps;
     if (left >= kGraphSteps) {
-        cudaGraphExec_t g = batch_graph(b, nitems, nshots);
+        int64_t kernels = 0;
+        cudaGraphExec_t g = batch_graph(b, nitems, nshots, &kernels);
         if (!g) return bfail(b, POE_ECUDA, "batch graph capture failed");
         for (; left >= kGraphSteps; left -= kGraphSteps) {
             BK(cudaGraphLaunch(g, b->stream));
-            b->launches += (b->span ? 1 : kGraphSteps) + 1;
+            b->launches += kernels;
         }
     }
     return left > 0 ? batch_steps(b, nitems, nshots, left) : POE_OK;
@@ -1509,12 +1530,13 @@ int poe_batch_run(poe_batch *b, const int64_t *nsteps)
 int poe_batch_tune_span(poe_batch *b, int32_t span)
 {
     if (!b) return POE_EINVAL;
-    if (span != 0 && span != 1) return bfail(b, POE_EINVAL, "tuning: span must be 0 or 1");
-    if ((span != 0) != b->span) {
+    if (span != POE_SPAN_NEVER && span != POE_SPAN_ALWAYS && span != POE_SPAN_AUTO)
+        return bfail(b, POE_EINVAL, "tuning: span must be POE_SPAN_NEVER, POE_SPAN_ALWAYS or POE_SPAN_AUTO");
+    if (span != b->span) {
         BK(cudaStreamSynchronize(b->stream));   // a graph still running holds the old launches
         drop_batch_graphs(b);
     }
-    b->span = span != 0;
+    b->span = span;
     return POE_OK;
 }
 

@@ -470,7 +470,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             }
             unsigned char *buf = smp + b * BUF_BYTES;
             if (lane == 0) {
-                if (MS) fence_proxy_async_global();   // the neighbours' stores, acquired above, before the copies
+                if (MS && kk > k) fence_proxy_async_global();   // the neighbours' stores, acquired above, before the copies
                 // the big copies first: the 4 velocity planes with a 4-cell halo and
                 // the 5 state planes with a 2-row halo, one box each (bytes
                 // announced, no arrival yet)

@@ -237,9 +237,11 @@ class Solver:
         dealt for an even share of edge tiles per CTA) and graph length."""
         self._check(L.lib().poe_tune(self.h, int(order), int(graph_steps)))
 
-    def tune_span(self, span=1):
-        """1: one step-spanning launch per captured graph (tiles of a step start as
-        soon as their neighbourhood finished the previous one); 0: a launch per step."""
+    def tune_span(self, span=L.SPAN_AUTO):
+        """1 (SPAN_ALWAYS): one step-spanning launch per captured graph (tiles of a
+        step start as soon as their neighbourhood finished the previous one); 0
+        (SPAN_NEVER): a launch per step; 2 (SPAN_AUTO, the default): spanning when
+        a step holds at most 24 tiles per SM."""
         self._check(L.lib().poe_tune_span(self.h, int(span)))
 
     def autotune(self, trial_steps=128):
@@ -328,8 +330,9 @@ class Batch:
         self._live()
         self._check(L.lib().poe_batch_sync(self.h))
 
-    def tune_span(self, span=1):
-        """Step-spanning launches for the batch (see Solver.tune_span)."""
+    def tune_span(self, span=L.SPAN_AUTO):
+        """Step-spanning launches for the batch (see Solver.tune_span; AUTO decides
+        per run segment, by the tiles of the models still stepping)."""
         self._live()
         self._check(L.lib().poe_batch_tune_span(self.h, int(span)))
 

@@ -34,8 +34,8 @@ CONSTANTS = ["POE_OK", "POE_EINVAL", "POE_ECFL", "POE_ENONFINITE", "POE_ETIMEOUT
              "POE_EIO", "POE_ESTATE", "POE_SRC_REF_DGAUSS_P", "POE_SRC_RICKER_FZ", "POE_REC_NONE", "POE_REC_VX",
              "POE_REC_VZ", "POE_REC_P", "POE_CTX_FAST_STENCIL", "POE_CTX_NO_PALETTE", "POE_NCOEF", "POE_NFIELDS",
              "POE_ORDER_ROWS", "POE_ORDER_COLUMNS", "POE_ORDER_TILE_MAJOR", "POE_ORDER_BALANCED",
-             "POE_AUTOTUNE_CANDIDATES", "POE_CHECKPOINT_VERSION", "POE_SG_MAP", "POE_SG_MAP_CH",
-             "POE_SG_SCALARS", "POE_SG_SAMPLES", "POE_SG_CHANNELS"]
+             "POE_AUTOTUNE_CANDIDATES", "POE_CHECKPOINT_VERSION", "POE_SPAN_NEVER", "POE_SPAN_ALWAYS",
+             "POE_SPAN_AUTO", "POE_SG_MAP", "POE_SG_MAP_CH", "POE_SG_SCALARS", "POE_SG_SAMPLES", "POE_SG_CHANNELS"]
 CONSTANTS += ["POE_C_RHO", "POE_C_RHOF", "POE_C_RSM", "POE_C_EOK", "POE_C_LAMBDAC", "POE_C_MU", "POE_C_ALPHA",
               "POE_C_RBM"]
 CONSTANTS += ["POE_MAX_MATERIALS", "POE_MROW", "POE_M_CO", "POE_M_C1", "POE_M_C2", "POE_M_RHOF_EOK", "POE_M_RCO",
@@ -108,6 +108,8 @@ def test_constants_match_python(header_facts):
     assert (L.ORDER_ROWS, L.ORDER_COLUMNS, L.ORDER_TILE_MAJOR, L.ORDER_BALANCED) == (
         c["POE_ORDER_ROWS"], c["POE_ORDER_COLUMNS"], c["POE_ORDER_TILE_MAJOR"], c["POE_ORDER_BALANCED"]) == (0, 1, 2, 3)
     assert L.AUTOTUNE_CANDIDATES == c["POE_AUTOTUNE_CANDIDATES"] == 4 * 2 * 2
+    assert (L.SPAN_NEVER, L.SPAN_ALWAYS, L.SPAN_AUTO) == (
+        c["POE_SPAN_NEVER"], c["POE_SPAN_ALWAYS"], c["POE_SPAN_AUTO"]) == (0, 1, 2)
     assert L.CHECKPOINT_VERSION == c["POE_CHECKPOINT_VERSION"]
     assert (S.MAP, S.MAP_CH, S.SCALARS, S.SAMPLES, S.CHANNELS) == (
         c["POE_SG_MAP"], c["POE_SG_MAP_CH"], c["POE_SG_SCALARS"], c["POE_SG_SAMPLES"], c["POE_SG_CHANNELS"])

@@ -63,7 +63,38 @@ def test_tuning_arguments_are_checked(poe):
         with pytest.raises(poe.PoeError):
             s.tune(0, 0)
         with pytest.raises(poe.PoeError):
-            s.tune_span(2)
+            s.tune_span(3)
         s.run(5)
         with pytest.raises(poe.PoeError):
             s.autotune(8)                     # shots not at step 0
+
+
+def test_span_auto_spans_steps_of_few_tiles_only(poe):
+    """POE_SPAN_AUTO (the default): one spanning launch per 64-step graph for a
+    step of few tiles per SM (one 1500 x 2000 shot, about 1600 tiles, about 10
+    per SM), one launch per step for a step of many (4 such shots, about 40 per
+    SM); SPAN_ALWAYS and SPAN_NEVER override it."""
+    import torch
+    assert poe.SPAN_AUTO == 2
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    frame = dict(rho_s=2650.0, phi=0.2, k_s=37e9, k_frame=10e9, mu_frame=8e9, kappa=1e-12, tortuosity=2.0)
+    water = poe.biot_material(rho_f=1000.0, k_f=2.25e9, eta=1e-3, **frame)
+    NX, NZ = 1499, 1999
+    coef, vp = poe.coeffs_biot([water], np.zeros((NZ + 1, NX + 1), np.uint8))
+    g = poe.grid(NX, NZ, 0.5, 5e-5)
+    px, pz = poe.pml_profiles(g, 20, 200.0, vp)
+    rec = [(x, 30, poe.REC_VZ) for x in range(100, 1400, 100)]
+    tiles = -(-(NX + 1) // 60) * -(-(NZ + 1) // 32)
+    for nshots, span, per_graph in ((1, None, 2), (4, None, 65), (4, poe.SPAN_ALWAYS, 2), (1, poe.SPAN_NEVER, 65)):
+        assert (nshots * tiles <= 24 * sms) == (nshots == 1)
+        with poe.Solver(g, coef, px, pz, fast=True) as s:
+            for k in range(nshots):
+                s.add_shot(poe.source(300 + 300 * k, 40, poe.SRC_RICKER_FZ, 200.0, 1e3, 0.0), rec)
+            if span is not None:
+                s.tune_span(span)
+            s.run(64)
+            s.sync()
+            n0 = s.launches
+            s.run(128)
+            s.sync()
+            assert s.launches - n0 == 2 * per_graph, (nshots, span)
