@@ -162,10 +162,10 @@ def leg_shots(P, stream, fast, nsteps=10000, nshots=64, single_shots=2):
 
 
 def leg_orders(P, stream, fast, nsteps=2000, reps=3):
-    """Work-list orders of the step kernel: rows (the default) against
-    balanced (the same tiles dealt so every CTA of the persistent launch gets
-    an even share of edge tiles), on the benchmark shot and on one 1001x1001
-    shot.  One solver per order, each warmed once; the orders alternate over
+    """Work-list orders of the step kernel: rows (the default with FAST
+    stencils) against balanced (the same tiles with the edge tiles spread
+    evenly through the list; the EXACT default), on the benchmark shot and on
+    one 1001x1001 shot.  One solver per order, each warmed once; the orders alternate over
     reps runs of nsteps steps from a reset shot.  Results must be equal bit
     for bit: only the order of independent tiles differs."""
     from poe2d_gb300 import _lib as L

@@ -282,16 +282,18 @@ typedef struct poe_checkpoint_header {
 int poe_checkpoint_info(const void *host_buf, int64_t size, poe_checkpoint_header *out);
 
 /* Tuning (no reference counterpart).  The step kernel walks a list of
- * (shot, tile) items, one CTA per SM; the order of that list decides which
- * tiles run side by side (halo reuse in L2), and poe_run replays a captured
- * CUDA graph of graph_steps steps.  Results do not depend on either. */
+ * (shot, tile) items, one CTA per SM, each CTA taking the next item from a
+ * shared counter; the order of that list decides which tiles run side by
+ * side (halo reuse in L2), and poe_run replays a captured CUDA graph of
+ * graph_steps steps.  Results do not depend on either. */
 enum {
-    POE_ORDER_ROWS = 0,       /* per shot, tile rows */
+    POE_ORDER_ROWS = 0,       /* per shot, tile rows; the default with FAST stencils */
     POE_ORDER_COLUMNS = 1,    /* per shot, tile columns */
     POE_ORDER_TILE_MAJOR = 2, /* the same tile of every shot side by side */
-    POE_ORDER_BALANCED = 3    /* rows, dealt so that every CTA of the persistent launch gets an
-                                 even share of edge tiles (C-PML strips, grid edges, the source:
-                                 about twice an interior tile's work); the default */
+    POE_ORDER_BALANCED = 3    /* rows, with the edge tiles (C-PML strips, grid edges, the source:
+                                 about twice an interior tile's work) spread evenly through the
+                                 list, so that edge and interior tiles are in flight together;
+                                 the default with EXACT stencils */
 };
 int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 

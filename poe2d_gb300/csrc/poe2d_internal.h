@@ -111,22 +111,23 @@ struct StreamShot {
 // shots over the work list items[0..nitems) of (0, shot, x0, z0).  nk = 1:
 // one launch per step.  nk > 1: one step-spanning launch, in which a tile of
 // step n > its first starts once its 3 x 3 neighbourhood has completed step
-// n-1 (the shots' done flags)
+// n-1 (the shots' done flags).  queue: 2 device ints, zero before the first
+// launch; each launch's CTAs take its items from it and set it back to zero
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     int nk, bool exact, bool kone, void *stream);
+                     int nk, bool exact, bool kone, int *queue, void *stream);
 // one step over several models: items (model, shot, x0, z0) index models_dev and shots_dev;
 // exact_few: every model's spacings have a 24 h of few bits; coef: the models read
 // their 8 coefficient planes per cell (all of them), else each has a material palette
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      int nk, bool exact, bool exact_few, bool coef, bool kone, void *stream);
+                      int nk, bool exact, bool exact_few, bool coef, bool kone, int *queue, void *stream);
 // the step kernel of one stencil mode (poe2d_tile_fast.cu, poe2d_tile_exact.cu,
 // poe2d_tile_exact_any.cu): models null for a single model m, else a batch
 int tile_step_fast(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                   int k, int nk, bool kone, bool coef, void *stream);
+                   int k, int nk, bool kone, bool coef, int *queue, void *stream);
 int tile_step_exact(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                    int k, int nk, bool kone, bool coef, void *stream);
+                    int k, int nk, bool kone, bool coef, int *queue, void *stream);
 int tile_step_exact_any(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-                        int nitems, int k, int nk, bool kone, bool coef, void *stream);
+                        int nitems, int k, int nk, bool kone, bool coef, int *queue, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
 // one thread waits, polls times at most, on an mbarrier no thread arrives at;

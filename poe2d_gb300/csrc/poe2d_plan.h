@@ -1,22 +1,22 @@
-// poe2d_plan.h -- load-balanced work-list order for the persistent step
-// kernel (host code, no CUDA types).
+// poe2d_plan.h -- the balanced work-list order of the persistent step kernel
+// (host code, no CUDA types).
 //
-// The step kernel runs `slots` CTAs; CTA b takes the items at positions b,
-// b + slots, b + 2 slots, ... of the work list, and a step ends when the
-// busiest CTA is done.  Edge tiles (a grid edge, a C-PML strip or the source
-// within reach of the tile and its halo) take about twice the work of an
-// interior tile, so in rows order the CTAs that happen to draw several edge
-// tiles set the step time: with one 2001^2 shot (2142 tiles, 313 of them
-// edge tiles) on 152 CTAs the busiest CTA has 19 units of work against a mean
-// of 16.2.
+// The step kernel's CTAs take the items of its work list in order, each the
+// next one from a shared counter.  Edge tiles (a grid edge, a C-PML strip or
+// the source within reach of the tile and its halo) take about twice the work
+// of an interior tile and wait on global loads of the C-PML memory; in rows
+// order they come in runs (a 2001^2 shot's first two and last two tile rows
+// are all edge tiles: 313 of its 2142 tiles), during which every SM is on the
+// strips.
 //
-// balanced_order() deals the same items so that every CTA's work (1 per
-// tile, 1 more per edge tile) is as even as the counts allow: CTAs with one
-// position fewer take more edge tiles (water-filling), each CTA's edge tiles
-// are spread evenly over its positions (Bresenham), and edge and interior
-// tiles each keep their order, so the tiles that run side by side stay
-// neighbours (their halos are shared through L2).  The result is a
-// permutation: position p holds item order[p].  Tiles are independent within
+// balanced_order() spreads them evenly through the list: with `slots`
+// positions per round (the SM count), the edge tiles go to the positions a
+// water-filling deal of them over the slots gives (so that with one CTA per
+// slot each CTA's work, 1 per tile and 1 more per edge tile, is as even as the
+// counts allow), each slot's spread evenly over its positions (Bresenham), and
+// edge and interior tiles each keep their order, so the tiles that run side
+// by side stay neighbours (their halos are shared through L2).  The result is
+// a permutation: position p holds item order[p].  Tiles are independent within
 // a step, so any order gives the same results bit for bit.
 #pragma once
 #include <stdint.h>

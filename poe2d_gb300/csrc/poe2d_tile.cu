@@ -23,30 +23,30 @@ int stencil_mode(bool exact, bool few)
 }
 
 int step_mode(int sm, const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-              int nitems, int k, int nk, bool kone, bool coef, void *stream)
+              int nitems, int k, int nk, bool kone, bool coef, int *queue, void *stream)
 {
     switch (sm) {
-    case SM_FAST: return tile_step_fast(m, models, shots, items, nitems, k, nk, kone, coef, stream);
-    case SM_EXACT_FEW: return tile_step_exact(m, models, shots, items, nitems, k, nk, kone, coef, stream);
-    default: return tile_step_exact_any(m, models, shots, items, nitems, k, nk, kone, coef, stream);
+    case SM_FAST: return tile_step_fast(m, models, shots, items, nitems, k, nk, kone, coef, queue, stream);
+    case SM_EXACT_FEW: return tile_step_exact(m, models, shots, items, nitems, k, nk, kone, coef, queue, stream);
+    default: return tile_step_exact_any(m, models, shots, items, nitems, k, nk, kone, coef, queue, stream);
     }
 }
 }  // namespace
 
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     int nk, bool exact, bool kone, void *stream)
+                     int nk, bool exact, bool kone, int *queue, void *stream)
 {
     (void)nshots;
     return step_mode(stencil_mode(exact, m.qx.few_bits && m.qz.few_bits), m, nullptr, shots_dev, items, nitems, k,
-                     nk, kone, m.ids == nullptr, stream);
+                     nk, kone, m.ids == nullptr, queue, stream);
 }
 
 int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, const int4 *items, int nitems, int k,
-                      int nk, bool exact, bool exact_few, bool coef, bool kone, void *stream)
+                      int nk, bool exact, bool exact_few, bool coef, bool kone, int *queue, void *stream)
 {
     const ModelDev dummy{};
     return step_mode(stencil_mode(exact, exact_few), dummy, models_dev, shots_dev, items, nitems, k, nk, kone, coef,
-                     stream);
+                     queue, stream);
 }
 
 // the bounded wait on a phase that never completes (no thread arrives): the

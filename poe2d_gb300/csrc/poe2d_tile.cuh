@@ -152,8 +152,10 @@ constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
 constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
 constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
 constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
-constexpr int PAL_OFF_B = 2 * BUF_BYTES;
-constexpr size_t PAL_SMEM = PAL_OFF_B + 64;
+constexpr int PAL_OFF_B = 2 * BUF_BYTES;           // mbarriers and counters
+constexpr int PAL_OFF_R = PAL_OFF_B + 64;          // MS: the producer -> publisher ring
+constexpr int RING = 4;                            // ring slots
+constexpr size_t PAL_SMEM = PAL_OFF_R + 128;
 // every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
 constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
 static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
@@ -229,6 +231,10 @@ __device__ __forceinline__ int ld_acquire_cta(const int *p)
     asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
     return v;
 }
+__device__ __forceinline__ void st_release_cta(int *p, int v)
+{
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
 
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
@@ -258,6 +264,7 @@ struct ItemMeta {
     int src_off, src_where, src_on;
     float src_val, pacc;
     int x0, z0, interior;
+    int g;                     // the item's index in the launch; -1: the work list has ended
 };
 static_assert(sizeof(ItemMeta) <= 128, "item parameters fit their slot");
 
@@ -293,6 +300,14 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 
 }  // namespace tile
 
+// Work queue: the CTAs take the launch's items in order from one counter
+// (queue[0]; queue[1] counts the CTAs that found it exhausted, and the last
+// of them sets both back to 0 for the next launch), so the tiles that run at
+// the same time are neighbours in the work list however long the launch
+// (their halos meet in L2) and a CTA that drew heavy tiles simply takes
+// fewer.  Tiles are independent within a step: the results do not depend on
+// which CTA computes which tile.
+//
 // MS (step-spanning launch): the launch runs steps k .. k+nk-1 and walks
 // (step, tile) items step by step: item g is tile g % nitems of step
 // k + g / nitems.  Before the producer fills a buffer with a tile of step n it
@@ -306,7 +321,7 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
 __global__ void __launch_bounds__(MS ? tile::PNT + 32 : tile::PNT, 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
-           const int4 *__restrict__ items, int nitems, int k, int nk, int prefetch)
+           const int4 *__restrict__ items, int nitems, int k, int nk, int prefetch, int *__restrict__ queue)
 {
     using namespace tile;
     constexpr bool EXACT = SM != SM_FAST;
@@ -318,7 +333,17 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     // MS: compute-warp releases of each buffer, counted (monotonic, so the
     // publisher may lag behind the buffer's reuse without losing count)
     int *released = reinterpret_cast<int *>(full + 4);
+    // MS: the producer hands each item's tile flag and step to the publisher
+    // through a ring of RING slots (slot j % RING holds item j once its
+    // sequence number reads j + 1; a null flag ends the list), and refills a
+    // slot only after the publisher has taken its previous item (published)
+    int *published = released + 2;
+    int **ring_flag = reinterpret_cast<int **>(smp + PAL_OFF_R);
+    int *ring_val = reinterpret_cast<int *>(ring_flag + RING);
+    int *ring_seq = ring_val + RING;
     const int tid = threadIdx.x;
+    // the error flag for a failure no item can be named for (read where needed)
+    auto err0 = [&]() { return MULTI ? models[0].err : mp.err; };
 
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
@@ -326,6 +351,8 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             mbar_init(&empty[b], NW);
             released[b] = 0;
         }
+        *published = 0;
+        for (int r = 0; r < RING; ++r) ring_seq[r] = 0;
         mbar_fence_init();
     }
     __syncthreads();
@@ -339,27 +366,37 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
     // hold it up, and it holds up neither.
     if (MS && tid >= PCT + 32) {
         if (tid != PCT + 32) return;
-        int j = 0;
-        for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
-            const int b = j & 1;
-            const int4 it = items[g % nitems];
-            const ModelDev &m = MULTI ? models[it.x] : mp;
-            const StreamShot &S = shots[it.y];
-            int *flag = S.done + (it.w / QZ) * m.ntx + it.z / QX;
-            const int nval = (int)(*S.step + k + g / nitems + 1);
-            const int want = NW * ((j >> 1) + 1);   // releases of buffer b once item j is done
+        // polls sleep between reads: this warp shares its SM's issue slots with
+        // the compute warps, and a tile's flag is needed only steps later
+        for (int j = 0;; ++j) {
+            const int r = j % RING;
             int poll = 0;
-            while (ld_acquire_cta(&released[b]) < want)
+            while (ld_acquire_cta(&ring_seq[r]) != j + 1) {
                 if (++poll > (1 << 22)) {
-                    atomicExch(mp.err ? mp.err : models[it.x].err, 1);
+                    atomicExch(err0(), 1);
                     return;
                 }
+                __nanosleep(128);
+            }
+            int *flag = ring_flag[r];
+            const int nval = ring_val[r];
+            st_release_cta(published, j + 1);   // slot r may be refilled
+            if (!flag) return;
+            const int b = j & 1;
+            const int want = NW * ((j >> 1) + 1);   // releases of buffer b once item j is done
+            poll = 0;
+            while (ld_acquire_cta(&released[b]) < want) {
+                if (++poll > (1 << 22)) {
+                    atomicExch(err0(), 1);
+                    return;
+                }
+                __nanosleep(128);
+            }
             // the compute warps' global stores, acquired through the counter, are
             // released with the flag (to generic and TMA readers)
             fence_proxy_async_global();
             st_release(flag, nval);
         }
-        return;
     }
 
     // ------------------------------------------------------------ producer
@@ -367,7 +404,21 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         const int lane = tid - PCT;
         int j = 0;
         bool gave_up = false;
-        for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
+        // ring slot j % RING for item j (MS, lane 0), once the publisher has taken item j - RING
+        auto ring_put = [&](int jj, int *flag, int val) -> bool {
+            const int r = jj % RING;
+            for (int poll = 0; ld_acquire_cta(published) < jj - RING + 1; ++poll)
+                if (poll >= (1 << 20)) return false;
+            ring_flag[r] = flag;
+            ring_val[r] = val;
+            st_release_cta(&ring_seq[r], jj + 1);
+            return true;
+        };
+        int gnext = lane == 0 ? atomicAdd(queue, 1) : 0;
+        for (;; ++j) {
+            const int g = __shfl_sync(0xffffffffu, gnext, 0);
+            if (g >= total) break;
+            if (lane == 0) gnext = atomicAdd(queue, 1);   // the next item, fetched while this one is set up
             const int b = j & 1;
             const int w = MS ? g % nitems : g;
             const int kk = MS ? k + g / nitems : k;
@@ -406,6 +457,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 M.trace_row = rec_on ? S.trace + (n - 1) * S.nrec : nullptr;
                 M.x0 = x0;
                 M.z0 = z0;
+                M.g = g;
                 // interior: no grid edge, C-PML strip or source within the tile and its halo
                 int sx = -1000000, sz = -1000000;
                 if (S.src_off >= 0) {
@@ -461,6 +513,13 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 // lanes 0-8 acquired the flags, lane 0 issues the copies: the warp
                 // barrier orders the one after the other
                 __syncwarp();
+                // the item's tile flag and step, for the publisher
+                if (lane == 0 && !ring_put(j, S.done + (z0 / QZ) * m.ntx + x0 / QX, (int)nn)) gave_up = true;
+                if (__shfl_sync(0xffffffffu, (int)gave_up, 0)) {
+                    if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
+                    gave_up = true;
+                    break;
+                }
             }
             // buffer b free again: released by the compute warps
             if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
@@ -501,8 +560,34 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             }
             __syncwarp();
         }
-        // copies in flight land before the CTA may exit: the last two fills
-        for (int i = j - 2 < 0 ? 0 : j - 2; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
+        // the end of the work list, as item j of the buffers: once buffer j & 1 is
+        // free (its fill j - 2 then landed too), its parameters say so (and, MS,
+        // so does the ring)
+        int drain_from = j - 2;
+        if (!gave_up) {
+            const int b = j & 1;
+            if (j >= 2 && !mbar_wait(&empty[b], (uint32_t)(((j - 2) >> 1) & 1))) {
+                if (lane == 0) atomicExch(err0(), 1);
+            } else {
+                drain_from = j - 1;
+                if (lane == 0) {
+                    reinterpret_cast<ItemMeta *>(smp + b * BUF_BYTES + BUF_OFF_M)->g = -1;
+                    if (MS && !ring_put(j, nullptr, 0)) atomicExch(err0(), 1);
+                    mbar_arrive(&full[b]);
+                }
+            }
+        }
+        // the last CTA to find the queue exhausted sets it back for the next launch
+        if (lane == 0) {
+            __threadfence();
+            if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
+                __threadfence();
+                atomicExch(queue, 0);
+                atomicExch(queue + 1, 0);
+            }
+        }
+        // copies in flight land before the CTA may exit
+        for (int i = drain_from < 0 ? 0 : drain_from; i < j; ++i) mbar_wait(&full[i & 1], (uint32_t)((i >> 1) & 1));
         return;
     }
 
@@ -517,9 +602,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         for (int i = tid; i < mp.nmat * MT_W; i += PCT) t0[i] = mp.mtab[i];
         compute_sync();
     }
-    int j = 0;
-    for (int g = blockIdx.x; g < total; g += gridDim.x, ++j) {
-        const int w = MS ? g % nitems : g;
+    for (int j = 0;; ++j) {
         const int b = j & 1;
         unsigned char *buf = smp + b * BUF_BYTES;
         // No barrier here: warps run ahead into the item as soon as its data
@@ -528,9 +611,10 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         // mid-point barrier, which then ends every compute thread together.
         if (!mbar_wait(&full[b], (uint32_t)((j >> 1) & 1))) {
             compute_sync_and(false);
-            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
+            if (tid == 0) atomicExch(err0(), 1);
             return;
         }
+        if (reinterpret_cast<const ItemMeta *>(buf + BUF_OFF_M)->g < 0) break;   // every compute warp ends here
         const ModelDev &m = MULTI ? *reinterpret_cast<const ModelDev *>(buf + BUF_OFF_MD) : mp;
         // the stencil divisors in registers: the model descriptor of a batch item
         // sits in shared memory, where the loops' own stores would force re-reads
@@ -895,7 +979,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             return true;
         };
         if (!(IM.interior ? compute(std::true_type{}) : compute(std::false_type{}))) {
-            if (tid == 0) atomicExch(MULTI ? models[items[w].x].err : mp.err, 1);
+            if (tid == 0) atomicExch(m.err, 1);
             return;
         }
         // hand buffer b back to the producer (and, MS, count the release for the
@@ -934,7 +1018,7 @@ inline int prefetch_strips(int nitems) { return nitems >= 8 * sm_count() ? 1 : 0
 // null) or a batch (models: device array; m unused)
 template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
 int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
-                int k, int nk, cudaStream_t st)
+                int k, int nk, int *queue, cudaStream_t st)
 {
     static std::atomic<uint64_t> done{0};
     auto kern = k_tile_pal<SM, KONE, MULTI, COEF, MS>;
@@ -954,18 +1038,18 @@ int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *sho
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return (int)cudaLaunchKernelEx(&cfg, kern, m, models, shots, items, nitems, k, MS ? nk : 1,
-                                   prefetch_strips(nitems));
+                                   prefetch_strips(nitems), queue);
 }
 
 // every (KONE, MULTI, COEF, step-spanning) variant of one stencil mode
 template <int SM>
 int tile_launch_mode(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
-                     int nitems, int k, int nk, bool kone, bool coef, cudaStream_t st)
+                     int nitems, int k, int nk, bool kone, bool coef, int *queue, cudaStream_t st)
 {
     const bool multi = models != nullptr;
     switch ((kone ? 8 : 0) | (multi ? 4 : 0) | (coef ? 2 : 0) | (nk > 1 ? 1 : 0)) {
 #define POE_TILE_CASE(s, KO, MU, CO, MS) \
-    case s: return tile_launch<SM, KO, MU, CO, MS>(m, models, shots, items, nitems, k, nk, st);
+    case s: return tile_launch<SM, KO, MU, CO, MS>(m, models, shots, items, nitems, k, nk, queue, st);
         POE_TILE_CASE(0, false, false, false, false) POE_TILE_CASE(1, false, false, false, true)
         POE_TILE_CASE(2, false, false, true, false) POE_TILE_CASE(3, false, false, true, true)
         POE_TILE_CASE(4, false, true, false, false) POE_TILE_CASE(5, false, true, false, true)
