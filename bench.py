@@ -682,7 +682,9 @@ def main():
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_step": alg, "step_us": step_s * 1e6,
                          "palette_min_bytes_per_step": alg_pal,
-                         "palette_frac": alg_pal / step_s / 1e9 / hbm},
+                         "palette_frac": alg_pal / step_s / 1e9 / hbm,
+                         "per": "time step: one step-spanning launch of the step kernel runs 64 steps; "
+                                "traffic = ncu's DRAM bytes of a warm launch / 64"},
             "cpu_baseline": cb, "reference_gpu": ref_gpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk.summary(), "wall_s": wall, "finite": ok, "parity": parity, "batched": batched,
             "surrogate": surrogate, "orders": orders,

@@ -303,8 +303,9 @@ int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
  * has completed step n-1 (per-tile flags in device memory, bounded waits), so
  * the steps overlap instead of each ending on its slowest CTA;
  * POE_SPAN_NEVER launches the step kernel once per step; POE_SPAN_AUTO (the
- * default) spans when a step holds at most 24 tiles per SM (one 2001 x 2001
- * shot: 14), where the step tail it removes is a large share of the step.
+ * default) spans when a step holds at most 96 tiles per SM (one 2001 x 2001
+ * shot: 14; 16 shots of 1001 x 1001: 57), where the step tail it removes
+ * outweighs its per-tile costs.
  * Results do not depend on it. */
 enum { POE_SPAN_NEVER = 0, POE_SPAN_ALWAYS = 1, POE_SPAN_AUTO = 2 };
 int poe_tune_span(poe_ctx *ctx, int32_t span);

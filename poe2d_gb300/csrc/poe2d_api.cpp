@@ -27,10 +27,11 @@ using namespace poe;
 namespace {
 constexpr int kGraphSteps = 64;
 // POE_SPAN_AUTO: step-spanning launches for steps of at most this many tiles
-// per SM (measured: a 2001^2 shot, 14 per SM, +13 %; one 1001^2 shot, 3.6, +29 %;
-// 16 shots of 1001^2, 57 per SM, -11 %: with many tiles per step the step tail
-// the spanning removes is small and its per-tile costs remain)
-constexpr int kSpanTilesPerSM = 24;
+// per SM (measured against a launch per step: a 2001^2 shot, 14 per SM,
+// +22 %; one 1001^2 shot, 3.6 per SM, +78 %; 16 shots of 1001^2, 57 per SM,
+// +4 %; 64 shots of 1001^2, 229 per SM, -3 %: with many tiles per step the
+// step tail the spanning removes is small and its per-tile costs remain)
+constexpr int kSpanTilesPerSM = 96;
 }
 
 struct ShotHost {

@@ -241,7 +241,7 @@ class Solver:
         """1 (SPAN_ALWAYS): one step-spanning launch per captured graph (tiles of a
         step start as soon as their neighbourhood finished the previous one); 0
         (SPAN_NEVER): a launch per step; 2 (SPAN_AUTO, the default): spanning when
-        a step holds at most 24 tiles per SM."""
+        a step holds at most 96 tiles per SM."""
         self._check(L.lib().poe_tune_span(self.h, int(span)))
 
     def autotune(self, trial_steps=128):

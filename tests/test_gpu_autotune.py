@@ -71,9 +71,9 @@ def test_tuning_arguments_are_checked(poe):
 
 def test_span_auto_spans_steps_of_few_tiles_only(poe):
     """POE_SPAN_AUTO (the default): one spanning launch per 64-step graph for a
-    step of few tiles per SM (one 1500 x 2000 shot, about 1600 tiles, about 10
-    per SM), one launch per step for a step of many (4 such shots, about 40 per
-    SM); SPAN_ALWAYS and SPAN_NEVER override it."""
+    step of at most 96 tiles per SM (one 1500 x 2000 shot, 1575 tiles, about
+    10 per SM), one launch per step for a step of more (10 such shots, about
+    104 per SM); SPAN_ALWAYS and SPAN_NEVER override it."""
     import torch
     assert poe.SPAN_AUTO == 2
     sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -85,11 +85,11 @@ def test_span_auto_spans_steps_of_few_tiles_only(poe):
     px, pz = poe.pml_profiles(g, 20, 200.0, vp)
     rec = [(x, 30, poe.REC_VZ) for x in range(100, 1400, 100)]
     tiles = -(-(NX + 1) // 60) * -(-(NZ + 1) // 32)
-    for nshots, span, per_graph in ((1, None, 2), (4, None, 65), (4, poe.SPAN_ALWAYS, 2), (1, poe.SPAN_NEVER, 65)):
-        assert (nshots * tiles <= 24 * sms) == (nshots == 1)
+    for nshots, span, per_graph in ((1, None, 2), (10, None, 65), (10, poe.SPAN_ALWAYS, 2), (1, poe.SPAN_NEVER, 65)):
+        assert (nshots * tiles <= 96 * sms) == (nshots == 1)
         with poe.Solver(g, coef, px, pz, fast=True) as s:
             for k in range(nshots):
-                s.add_shot(poe.source(300 + 300 * k, 40, poe.SRC_RICKER_FZ, 200.0, 1e3, 0.0), rec)
+                s.add_shot(poe.source(300 + 100 * k, 40, poe.SRC_RICKER_FZ, 200.0, 1e3, 0.0), rec)
             if span is not None:
                 s.tune_span(span)
             s.run(64)
