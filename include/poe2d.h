@@ -310,13 +310,25 @@ int poe_tune(poe_ctx *ctx, int32_t order, int32_t graph_steps);
 enum { POE_SPAN_NEVER = 0, POE_SPAN_ALWAYS = 1, POE_SPAN_AUTO = 2 };
 int poe_tune_span(poe_ctx *ctx, int32_t span);
 
-/* Time every (order, graph_steps in {16, 64}, span NEVER or ALWAYS) candidate on
- * this context for trial_steps steps, keep the fastest and report it;
- * ms_out (may be NULL) receives the POE_AUTOTUNE_CANDIDATES timings,
- * candidate c = order c / 4, graph_steps {16, 64}[(c / 2) % 2], span c % 2.
- * Every shot must be at step 0; the shots are reset to step 0 afterwards;
+/* The step kernel's tile height (no reference counterpart): 60 x 32 tiles
+ * (the default; every kernel variant) or 60 x 16 (FAST stencils, a context
+ * outside any batch: twice the tiles per step, for grids too small to keep
+ * every SM busy).  Results do not depend on it.  POE_EINVAL for another
+ * height or 16 with EXACT stencils, POE_ESTATE for a context in a batch. */
+int poe_tune_tile(poe_ctx *ctx, int32_t tile_z);
+
+/* The context's current tuning; any pointer may be NULL. */
+int poe_tuning(const poe_ctx *ctx, int32_t *order, int32_t *graph_steps, int32_t *span, int32_t *tile_z);
+
+/* Time every (tile height, order, graph_steps in {16, 64}, span NEVER or
+ * ALWAYS) candidate on this context for trial_steps steps, keep the fastest
+ * and report it; ms_out (may be NULL) receives the POE_AUTOTUNE_CANDIDATES
+ * timings, candidate c = tile height {32, 16}[c / 16], order (c / 4) % 4,
+ * graph_steps {16, 64}[(c / 2) % 2], span c % 2 (-1 for a 16-row candidate
+ * the context cannot take: EXACT stencils or a batch member).  Every shot
+ * must be at step 0; the shots are reset to step 0 afterwards; poe_tune_tile,
  * poe_tune and poe_tune_span then hold the winner. */
-enum { POE_AUTOTUNE_CANDIDATES = 16 };
+enum { POE_AUTOTUNE_CANDIDATES = 32 };
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out);
 
 /* Steps completed by a shot. */

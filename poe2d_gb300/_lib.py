@@ -19,7 +19,7 @@ CTX_FAST_STENCIL = 1
 CTX_NO_PALETTE = 2
 MAX_MATERIALS, MROW = 64, 14
 ORDER_ROWS, ORDER_COLUMNS, ORDER_TILE_MAJOR, ORDER_BALANCED = range(4)
-AUTOTUNE_CANDIDATES = 16
+AUTOTUNE_CANDIDATES = 32
 SPAN_NEVER, SPAN_ALWAYS, SPAN_AUTO = range(3)
 M_CO, M_C1, M_C2, M_RHOF_EOK, M_RCO, M_RC1 = range(8, 14)
 FIELDS = ["vx", "vz", "wx", "wz", "sxx", "szz", "sxz", "p", "g11", "g22", "xi1", "xi2"]
@@ -106,6 +106,9 @@ SYMBOLS = {
     "poe_checkpoint_info": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CheckpointHeader)]),
     "poe_tune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "poe_tune_span": (C.c_int, [C.c_void_p, C.c_int32]),
+    "poe_tune_tile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "poe_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                             C.POINTER(C.c_int32)]),
     "poe_batch_tune_span": (C.c_int, [C.c_void_p, C.c_int32]),
     "poe_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _fp]),
     "poe_steps_done": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),

@@ -21,7 +21,7 @@ LIB = os.path.join(BUILD, "libpoe2d.so")
 CLI = os.path.join(BUILD, "poe2d_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["poe2d_tile_fast.cu", "poe2d_tile_exact.cu", "poe2d_tile_exact_any.cu", "poe2d_tile.cu", "poe2d_api.cpp",
+SOURCES = ["poe2d_tile_fast.cu", "poe2d_tile_exact.cu", "poe2d_tile_exact_any.cu", "poe2d_tile_fast16.cu", "poe2d_tile.cu", "poe2d_api.cpp",
            "poe2d_setup.cpp", "sg_gemm.cu", "sg_ops.cu", "sg_net.cpp"]
 
 

@@ -36,12 +36,15 @@ constexpr int kSpanTilesPerSM = 96;
 
 struct ShotHost {
     float *f[2] = {nullptr, nullptr};       // NSF planes each, one allocation (f[0])
-    CUtensorMap *tm = nullptr;              // device copies: [0] velocity box, [1] state box
+    // device copies of the tile boxes: [0] velocity, [1] state for 32-row
+    // tiles, [2], [3] the same for PAL_TZ_SMALL-row tiles
+    CUtensorMap *tm = nullptr;
     float *mx[2] = {nullptr, nullptr}, *mz[2] = {nullptr, nullptr};
     float *mxv = nullptr, *mzv = nullptr, *acc = nullptr;
     float *src_tab = nullptr, *trace = nullptr;
-    int *rec_start = nullptr;
-    int4 *rec_sorted = nullptr;
+    // receivers as CSR over tiles, for each tile height ([0] PAL_TZ, [1] PAL_TZ_SMALL)
+    int *rec_start[2] = {nullptr, nullptr};
+    int4 *rec_sorted[2] = {nullptr, nullptr};
     int nrec = 0;
     int64_t trace_cap = 0;
     int64_t src_cap = 0;     // entries computed in src_tab
@@ -52,7 +55,8 @@ struct ShotHost {
     int src_where = SRC_NONE;
     int64_t steps = 0;
     uint64_t rec_hash = 0;   // of the receiver list (checkpoint identity)
-    int *done = nullptr;     // per tile: a step it has completed (step-spanning launches)
+    int *done = nullptr;     // per tile: a step it has completed (step-spanning launches); sized for
+                             // the smaller tile height's tiling
 };
 
 struct poe_ctx {
@@ -83,11 +87,12 @@ struct poe_ctx {
     CUtensorMap *tm_model = nullptr;   // palette mode: TMA descriptors of ids, px, pz (device)
     float *mtab = nullptr;      // palette mode: material table
     int nmat = 0;
-    int ntx = 1, ntz = 1;       // tiles across x and z
+    int ntx = 1, ntz = 1;       // tiles across x and z (at the context's tile height)
+    int ncell_max = 1;          // tiles at the smaller tile height (the shots' flag arrays)
     int order = POE_ORDER_ROWS;      // work-list order (POE_ORDER_*; EXACT contexts start BALANCED)
     int graph_steps = kGraphSteps;   // steps per captured graph
     int span = POE_SPAN_AUTO;        // step-spanning launches (POE_SPAN_*)
-    int tile_x = PAL_TX, tile_z = PAL_TZ;
+    int tile_x = PAL_TX, tile_z = PAL_TZ;   // the step kernel's tile (tile_z: PAL_TZ or PAL_TZ_SMALL)
     poe_batch *batch = nullptr;   // the batch this context belongs to, if any
     uint64_t prof_hash = 0;       // of the C-PML profiles given to poe_create
     uint64_t coef_hash = 0;       // of the 8 coefficient planes, computed on first checkpoint use
@@ -154,8 +159,10 @@ void free_shot(ShotHost &s)
     cudaFree(s.acc);
     cudaFree(s.src_tab);
     cudaFree(s.trace);
-    cudaFree(s.rec_start);
-    cudaFree(s.rec_sorted);
+    for (int t = 0; t < 2; ++t) {
+        cudaFree(s.rec_start[t]);
+        cudaFree(s.rec_sorted[t]);
+    }
     cudaFree(s.done);
     s = ShotHost{};
 }
@@ -199,12 +206,28 @@ bool tile_is_edge(const poe_ctx *ctx, int shot, int x0, int z0)
 {
     const ModelDev &m = ctx->m;
     const ShotHost &s = ctx->shots[(size_t)shot];
-    const int xa = x0 - 2, xb = x0 + PAL_TX + 1, za = z0 - 2, zb = z0 + PAL_TZ + 1;
+    const int xa = x0 - 2, xb = x0 + ctx->tile_x + 1, za = z0 - 2, zb = z0 + ctx->tile_z + 1;
     const bool src_in = s.src_where != SRC_NONE && s.src.ix >= xa && s.src.ix <= xb && s.src.iz >= za &&
                         s.src.iz <= zb;
     const bool interior = xa >= 2 && xa >= m.xL && xb <= m.NX - 2 && xb < m.xR && za >= 2 && za >= m.zT &&
                           zb <= m.NZ - 2 && zb < m.zB && !src_in;
     return !interior;
+}
+
+// the step kernel's tile height (PAL_TZ or PAL_TZ_SMALL): tile counts and the
+// model's id and z-profile boxes; the work list and the shots' tile data
+// follow at the next sync
+void set_tile(poe_ctx *ctx, int tz)
+{
+    const int nz = ctx->g.NZ + 1;
+    const int t = tz == PAL_TZ ? 0 : 1;
+    ctx->tile_z = tz;
+    ctx->ntz = (nz + tz - 1) / tz;
+    ctx->m.ntx = ctx->ntx;
+    ctx->m.ntz = ctx->ntz;
+    ctx->m.tm_ids = ctx->tm_model && ctx->ids ? (const void *)&ctx->tm_model[t ? 3 : 0] : nullptr;
+    ctx->m.tm_pz = ctx->tm_model ? (const void *)&ctx->tm_model[t ? 4 : 2] : nullptr;
+    ctx->shots_dirty = true;
 }
 
 int sync_shots(poe_ctx *ctx)
@@ -241,13 +264,14 @@ int sync_shots(poe_ctx *ctx)
         d.src_where = s.src_where;
         d.src_n = s.src_n;
         d.src_tab = s.src_tab;
-        d.rec_start = s.rec_start;
-        d.rec_sorted = s.rec_sorted;
+        const int ti = ctx->tile_z == PAL_TZ ? 0 : 1;
+        d.rec_start = s.rec_start[ti];
+        d.rec_sorted = s.rec_sorted[ti];
         d.nrec = s.nrec;
         d.trace = s.trace;
         d.trace_cap = s.trace_cap;
-        d.tm_v = s.tm ? (const void *)&s.tm[0] : nullptr;
-        d.tm_s = s.tm ? (const void *)&s.tm[1] : nullptr;
+        d.tm_v = s.tm ? (const void *)&s.tm[2 * ti] : nullptr;
+        d.tm_s = s.tm ? (const void *)&s.tm[2 * ti + 1] : nullptr;
         d.done = s.done;
         st[i] = s.steps;
         ctx->max_rec = std::max(ctx->max_rec, s.nrec);
@@ -255,7 +279,9 @@ int sync_shots(poe_ctx *ctx)
     // step kernel work list: every tile of every shot, in the context's order
     ctx->items.clear();
     {
-        auto add = [&](int i, int tx, int tz) { ctx->items.push_back(make_int4(0, i, tx * PAL_TX, tz * PAL_TZ)); };
+        auto add = [&](int i, int tx, int tz) {
+            ctx->items.push_back(make_int4(0, i, tx * ctx->tile_x, tz * ctx->tile_z));
+        };
         if (ctx->order == POE_ORDER_TILE_MAJOR) {        // the same tile of every shot side by side
             for (int tz = 0; tz < ctx->ntz; ++tz)
                 for (int tx = 0; tx < ctx->ntx; ++tx)
@@ -363,7 +389,7 @@ int ensure_trace(poe_ctx *ctx, ShotHost &s, int64_t need)
 int step_launch(poe_ctx *ctx, int k, int nk)
 {
     return launch_tile_step(ctx->m, ctx->shots_dev, (int)ctx->shots.size(), ctx->items_dev, (int)ctx->items.size(), k,
-                            nk, ctx->exact, ctx->kone, ctx->queue_dev, ctx->stream);
+                            nk, ctx->exact, ctx->kone, ctx->tile_z, ctx->queue_dev, ctx->stream);
 }
 
 // the context's launches for nsteps steps (one step-spanning launch, or one
@@ -618,12 +644,18 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     if (rc == POE_OK) {
         // the step kernel's producer fetches each tile's ids (palette models)
         // and profile slices with TMA (rows of P bytes / P floats / R floats)
-        CUtensorMap tm[3];
+        // [0] ids, [1] x profiles, [2] z profiles for 32-row tiles; [3] ids, [4] z
+        // profiles for PAL_TZ_SMALL-row tiles
+        CUtensorMap tm[5];
         std::memset(tm, 0, sizeof(tm));
-        bool ok = (!ctx->ids ||
-                   encode_2d(&tm[0], CU_TENSOR_MAP_DATA_TYPE_UINT8, ctx->ids, m.P, m.R, m.P, PAL_IDS_W, PAL_IDS_H)) &&
-                  encode_2d(&tm[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->px, m.P, 6, (int64_t)m.P * 4, TMA_VW, 6) &&
-                  encode_2d(&tm[2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->pz, m.R, 6, (int64_t)m.R * 4, TMA_VH, 6);
+        bool ok = encode_2d(&tm[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->px, m.P, 6, (int64_t)m.P * 4, TMA_VW, 6);
+        for (int t = 0; t < 2 && ok; ++t) {
+            const int tz = t ? PAL_TZ_SMALL : PAL_TZ;
+            ok = (!ctx->ids || encode_2d(&tm[t ? 3 : 0], CU_TENSOR_MAP_DATA_TYPE_UINT8, ctx->ids, m.P, m.R, m.P,
+                                         PAL_IDS_W, tile_ids_h(tz))) &&
+                 encode_2d(&tm[t ? 4 : 2], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ctx->pz, m.R, 6, (int64_t)m.R * 4,
+                           tile_vh(tz), 6);
+        }
         cudaError_t e = ok ? cudaMalloc(&ctx->tm_model, sizeof(tm)) : cudaErrorInvalidValue;
         if (e == cudaSuccess) e = cudaMemcpy(ctx->tm_model, tm, sizeof(tm), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) rc = fail(ctx, POE_ECUDA, std::string("TMA descriptors: ") + cudaGetErrorString(e));
@@ -639,16 +671,12 @@ int poe_create(const poe_grid *grid, const float *coef, const float *prof_x, con
     m.ids = ctx->ids;
     m.mtab = ctx->mtab;
     m.nmat = ctx->nmat;
-    m.tm_ids = ctx->tm_model && ctx->ids ? (const void *)&ctx->tm_model[0] : nullptr;
     m.tm_px = ctx->tm_model ? (const void *)&ctx->tm_model[1] : nullptr;
-    m.tm_pz = ctx->tm_model ? (const void *)&ctx->tm_model[2] : nullptr;
-    // tile geometry of the step kernel (receiver lists are per tile)
+    // tile geometry of the step kernel (receiver lists and flags are per tile)
     ctx->tile_x = PAL_TX;
-    ctx->tile_z = PAL_TZ;
     ctx->ntx = (nx + ctx->tile_x - 1) / ctx->tile_x;
-    ctx->ntz = (nz + ctx->tile_z - 1) / ctx->tile_z;
-    ctx->m.ntx = ctx->ntx;
-    ctx->m.ntz = ctx->ntz;
+    ctx->ncell_max = ctx->ntx * ((nz + PAL_TZ_SMALL - 1) / PAL_TZ_SMALL);
+    set_tile(ctx, PAL_TZ);
     *out = ctx;
     return POE_OK;
 }
@@ -670,26 +698,28 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
         s.src_where = src->kind == POE_SRC_REF_DGAUSS_P ? SRC_P : SRC_FZ;
         s.src_off = (int64_t)(src->iz + ZH) * m.P + (src->ix + XH);
     }
-    // receivers: CSR over tiles, so each tile records its own
-    const int ncell = ctx->ntx * ctx->ntz;
-    std::vector<int> start((size_t)ncell + 1, 0);
-    std::vector<int4> sorted;
+    // receivers: CSR over tiles, so each tile records its own (for either tile height)
     for (int i = 0; i < nrec; ++i) {
         const poe_receiver &r = rec[i];
         if (r.comp == POE_REC_NONE) continue;
         if (r.comp < 0 || r.comp > 2 || r.ix < 0 || r.ix > NX || r.iz < 0 || r.iz > NZ)
             return fail(ctx, POE_EINVAL, "receiver " + std::to_string(i) + " outside the grid");
-        start[(size_t)(r.iz / ctx->tile_z) * ctx->ntx + r.ix / ctx->tile_x + 1]++;
     }
-    for (int c = 0; c < ncell; ++c) start[c + 1] += start[c];
-    sorted.resize((size_t)start[ncell]);
-    {
-        std::vector<int> fill(start.begin(), start.end() - 1);
+    std::vector<int> start[2];
+    std::vector<int4> sorted[2];
+    for (int t = 0; t < 2; ++t) {
+        const int tz = t ? PAL_TZ_SMALL : PAL_TZ;
+        const int ncell = ctx->ntx * ((NZ + tz) / tz);
+        start[t].assign((size_t)ncell + 1, 0);
+        for (int i = 0; i < nrec; ++i)
+            if (rec[i].comp != POE_REC_NONE) start[t][(size_t)(rec[i].iz / tz) * ctx->ntx + rec[i].ix / ctx->tile_x + 1]++;
+        for (int c = 0; c < ncell; ++c) start[t][c + 1] += start[t][c];
+        sorted[t].resize((size_t)start[t][ncell]);
+        std::vector<int> fill(start[t].begin(), start[t].end() - 1);
         for (int i = 0; i < nrec; ++i) {
             const poe_receiver &r = rec[i];
             if (r.comp == POE_REC_NONE) continue;
-            sorted[fill[(size_t)(r.iz / ctx->tile_z) * ctx->ntx + r.ix / ctx->tile_x]++] =
-                make_int4(r.ix, r.comp, i, r.iz);
+            sorted[t][fill[(size_t)(r.iz / tz) * ctx->ntx + r.ix / ctx->tile_x]++] = make_int4(r.ix, r.comp, i, r.iz);
         }
     }
     auto bad = [&](cudaError_t e, const char *what) {
@@ -705,12 +735,15 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     if ((e = cudaMemsetAsync(s.f[0], 0, 2 * fbytes, ctx->stream)) != cudaSuccess) return bad(e, "state");
     s.f[1] = s.f[0] + NSF * m.plane;
     {
-        CUtensorMap tm[2];
+        CUtensorMap tm[4];
         // the 4 velocity planes (SF_VX .. SF_WZ) and the 5 stress-state planes
-        // (SF_SXZ .. SF_XI2) of a tile, one copy each
-        if (!encode_planes(&tm[0], s.f[0], m, 2 * NSF, TMA_VW, TMA_VH, 4) ||
-            !encode_planes(&tm[1], s.f[0], m, 2 * NSF, TMA_VW, TMA_SH, 5))
-            return bad(cudaErrorInvalidValue, "TMA descriptor");
+        // (SF_SXZ .. SF_XI2) of a tile, one copy each, for either tile height
+        for (int t = 0; t < 2; ++t) {
+            const int tz = t ? PAL_TZ_SMALL : PAL_TZ;
+            if (!encode_planes(&tm[2 * t], s.f[0], m, 2 * NSF, TMA_VW, tile_vh(tz), 4) ||
+                !encode_planes(&tm[2 * t + 1], s.f[0], m, 2 * NSF, TMA_VW, tile_sh(tz), 5))
+                return bad(cudaErrorInvalidValue, "TMA descriptor");
+        }
         if ((e = cudaMalloc(&s.tm, sizeof(tm))) != cudaSuccess) return bad(e, "TMA descriptor");
         if ((e = cudaMemcpyAsync(s.tm, tm, sizeof(tm), cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
             return bad(e, "TMA descriptor");
@@ -735,17 +768,21 @@ int poe_add_shot(poe_ctx *ctx, const poe_source *src, const poe_receiver *rec, i
     }
     if ((e = cudaMalloc(&s.acc, sizeof(float) * 2)) != cudaSuccess) return bad(e, "acc");
     if ((e = cudaMemsetAsync(s.acc, 0, sizeof(float) * 2, ctx->stream)) != cudaSuccess) return bad(e, "acc");
-    if ((e = cudaMalloc(&s.done, sizeof(int) * ncell)) != cudaSuccess) return bad(e, "tile flags");
-    if ((e = cudaMemsetAsync(s.done, 0, sizeof(int) * ncell, ctx->stream)) != cudaSuccess) return bad(e, "tile flags");
-    if ((e = cudaMalloc(&s.rec_start, sizeof(int) * start.size())) != cudaSuccess) return bad(e, "receivers");
-    if ((e = cudaMemcpyAsync(s.rec_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice,
-                             ctx->stream)) != cudaSuccess)
-        return bad(e, "receivers");
-    if (!sorted.empty()) {
-        if ((e = cudaMalloc(&s.rec_sorted, sizeof(int4) * sorted.size())) != cudaSuccess) return bad(e, "receivers");
-        if ((e = cudaMemcpyAsync(s.rec_sorted, sorted.data(), sizeof(int4) * sorted.size(), cudaMemcpyHostToDevice,
-                                 ctx->stream)) != cudaSuccess)
+    if ((e = cudaMalloc(&s.done, sizeof(int) * ctx->ncell_max)) != cudaSuccess) return bad(e, "tile flags");
+    if ((e = cudaMemsetAsync(s.done, 0, sizeof(int) * ctx->ncell_max, ctx->stream)) != cudaSuccess)
+        return bad(e, "tile flags");
+    for (int t = 0; t < 2; ++t) {
+        if ((e = cudaMalloc(&s.rec_start[t], sizeof(int) * start[t].size())) != cudaSuccess) return bad(e, "receivers");
+        if ((e = cudaMemcpyAsync(s.rec_start[t], start[t].data(), sizeof(int) * start[t].size(),
+                                 cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
             return bad(e, "receivers");
+        if (!sorted[t].empty()) {
+            if ((e = cudaMalloc(&s.rec_sorted[t], sizeof(int4) * sorted[t].size())) != cudaSuccess)
+                return bad(e, "receivers");
+            if ((e = cudaMemcpyAsync(s.rec_sorted[t], sorted[t].data(), sizeof(int4) * sorted[t].size(),
+                                     cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+                return bad(e, "receivers");
+        }
     }
     s.nrec = nrec;
     {
@@ -927,7 +964,7 @@ int poe_reset_shot(poe_ctx *ctx, int32_t shot)
     if (s->mxv) CK(cudaMemsetAsync(s->mxv, 0, xbytes, ctx->stream));
     if (s->mzv) CK(cudaMemsetAsync(s->mzv, 0, zbytes, ctx->stream));
     CK(cudaMemsetAsync(s->acc, 0, sizeof(float) * 2, ctx->stream));
-    CK(cudaMemsetAsync(s->done, 0, sizeof(int) * ctx->ntx * ctx->ntz, ctx->stream));   // never ahead of the shot
+    CK(cudaMemsetAsync(s->done, 0, sizeof(int) * ctx->ncell_max, ctx->stream));   // never ahead of the shot
     if (s->trace) CK(cudaMemsetAsync(s->trace, 0, sizeof(float) * s->trace_cap * s->nrec, ctx->stream));
     s->steps = 0;
     ctx->shots_dirty = true;
@@ -1179,6 +1216,33 @@ int poe_tune_span(poe_ctx *ctx, int32_t span)
     return POE_OK;
 }
 
+int poe_tune_tile(poe_ctx *ctx, int32_t tile_z)
+{
+    if (!ctx) return POE_EINVAL;
+    if (tile_z != PAL_TZ && tile_z != PAL_TZ_SMALL)
+        return fail(ctx, POE_EINVAL, "tuning: tile_z must be 32 or 16");
+    if (tile_z == ctx->tile_z) return POE_OK;
+    if (tile_z == PAL_TZ_SMALL && ctx->exact)
+        return fail(ctx, POE_EINVAL, "tuning: 16-row tiles are built for FAST stencils only");
+    if (ctx->batch) return fail(ctx, POE_ESTATE, "tuning: the context belongs to a batch (32-row tiles)");
+    CK(cudaStreamSynchronize(ctx->stream));   // no launch still reads the old work list
+    drop_graph(ctx);
+    set_tile(ctx, tile_z);
+    // the flags are indexed by tile: start the new tiling from zero (never ahead of a shot)
+    for (ShotHost &sh : ctx->shots) CK(cudaMemsetAsync(sh.done, 0, sizeof(int) * ctx->ncell_max, ctx->stream));
+    return sync_shots(ctx);
+}
+
+int poe_tuning(const poe_ctx *ctx, int32_t *order, int32_t *graph_steps, int32_t *span, int32_t *tile_z)
+{
+    if (!ctx) return POE_EINVAL;
+    if (order) *order = ctx->order;
+    if (graph_steps) *graph_steps = ctx->graph_steps;
+    if (span) *span = ctx->span;
+    if (tile_z) *tile_z = ctx->tile_z;
+    return POE_OK;
+}
+
 int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t *graph_steps_out, float *ms_out)
 {
     if (!ctx || trial_steps < 1) return POE_EINVAL;
@@ -1192,10 +1256,19 @@ int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t 
     CK(cudaEventCreate(&e1));
     int best = -1, rc = POE_OK;
     float best_ms = 0.0f;
-    // candidate c: order c / 4, graph length kSteps[(c / 2) % 2], span c % 2
+    // 16-row tiles: FAST contexts outside a batch
+    const bool small_ok = !ctx->exact && !ctx->batch;
+    // candidate c: tile height {32, 16}[c / 16], order (c / 4) % 4, graph length
+    // kSteps[(c / 2) % 2], span c % 2
     for (int c = 0; c < POE_AUTOTUNE_CANDIDATES && rc == POE_OK; ++c) {
-        const int order = c / 4, gs = kSteps[(c / 2) % 2], span = c % 2;
-        if ((rc = poe_tune(ctx, order, gs)) != POE_OK || (rc = poe_tune_span(ctx, span)) != POE_OK) break;
+        const int tz = c / 16 ? PAL_TZ_SMALL : PAL_TZ, order = (c / 4) % 4, gs = kSteps[(c / 2) % 2], span = c % 2;
+        if (tz == PAL_TZ_SMALL && !small_ok) {
+            if (ms_out) ms_out[c] = -1.0f;    // not a candidate for this context
+            continue;
+        }
+        if ((rc = poe_tune_tile(ctx, tz)) != POE_OK || (rc = poe_tune(ctx, order, gs)) != POE_OK ||
+            (rc = poe_tune_span(ctx, span)) != POE_OK)
+            break;
         if ((rc = poe_run(ctx, gs)) != POE_OK) break;        // capture the graph, first touch
         cudaEventRecord(e0, ctx->stream);
         if ((rc = poe_run(ctx, trial_steps)) != POE_OK) break;
@@ -1217,9 +1290,10 @@ int poe_autotune(poe_ctx *ctx, int32_t trial_steps, int32_t *order_out, int32_t 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != POE_OK) return rc;
-    if ((rc = poe_tune(ctx, best / 4, kSteps[(best / 2) % 2])) != POE_OK) return rc;
+    if ((rc = poe_tune_tile(ctx, best / 16 ? PAL_TZ_SMALL : PAL_TZ)) != POE_OK) return rc;
+    if ((rc = poe_tune(ctx, (best / 4) % 4, kSteps[(best / 2) % 2])) != POE_OK) return rc;
     rc = poe_tune_span(ctx, best % 2);
-    if (order_out) *order_out = best / 4;
+    if (order_out) *order_out = (best / 4) % 4;
     if (graph_steps_out) *graph_steps_out = kSteps[(best / 2) % 2];
     return rc;
 }
@@ -1441,6 +1515,8 @@ int poe_batch_create(poe_ctx *const *ctxs, int32_t n, void *stream, poe_batch **
             return fail(ctxs[i], POE_EINVAL, "batch: palette models and per-cell coefficient models in one batch");
         if (ctxs[i]->device != ctxs[0]->device) return fail(ctxs[i], POE_EINVAL, "batch: contexts on other devices");
         if (ctxs[i]->exact != ctxs[0]->exact) return fail(ctxs[i], POE_EINVAL, "batch: mixed stencil modes");
+        if (ctxs[i]->tile_z != PAL_TZ)
+            return fail(ctxs[i], POE_EINVAL, "batch: a context tuned to 16-row tiles (batches run 32-row tiles)");
         for (int j = 0; j < i; ++j)
             if (ctxs[j] == ctxs[i]) return fail(ctxs[i], POE_EINVAL, "batch: context listed twice");
         if (ctxs[i]->batch) return fail(ctxs[i], POE_ESTATE, "batch: context already belongs to a batch");

@@ -112,9 +112,10 @@ struct StreamShot {
 // one launch per step.  nk > 1: one step-spanning launch, in which a tile of
 // step n > its first starts once its 3 x 3 neighbourhood has completed step
 // n-1 (the shots' done flags).  queue: 2 device ints, zero before the first
-// launch; each launch's CTAs take its items from it and set it back to zero
+// launch; each launch's CTAs take its items from it and set it back to zero.
+// tile_z: the tiles' height (PAL_TZ, or PAL_TZ_SMALL with FAST stencils)
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     int nk, bool exact, bool kone, int *queue, void *stream);
+                     int nk, bool exact, bool kone, int tile_z, int *queue, void *stream);
 // one step over several models: items (model, shot, x0, z0) index models_dev and shots_dev;
 // exact_few: every model's spacings have a 24 h of few bits; coef: the models read
 // their 8 coefficient planes per cell (all of them), else each has a material palette
@@ -128,19 +129,26 @@ int tile_step_exact(const ModelDev &m, const ModelDev *models, const StreamShot 
                     int k, int nk, bool kone, bool coef, int *queue, void *stream);
 int tile_step_exact_any(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
                         int nitems, int k, int nk, bool kone, bool coef, int *queue, void *stream);
+// the FAST single-model variants on 60 x PAL_TZ_SMALL tiles (poe2d_tile_fast16.cu)
+int tile_step_fast16(const ModelDev &m, const StreamShot *shots, const int4 *items, int nitems, int k, int nk,
+                     bool kone, bool coef, int *queue, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
 // one thread waits, polls times at most, on an mbarrier no thread arrives at;
 // sets *err when the wait gives up
 int launch_wait_limit(int *err, int polls, void *stream);
-// step kernel tile: 60 x 32 cells worked by 64 x 4 threads (stress on 64
-// columns = tile + 2-cell halo each side); TMA boxes of 68 x 40 (velocity) and
-// 68 x 36 (stress state) floats
-constexpr int PAL_TX = 60, PAL_TZ = 32;
-constexpr int TMA_VW = PAL_TX + 8, TMA_VH = PAL_TZ + 8, TMA_SH = PAL_TZ + 4;
-// material-id box: rows z0-2 .. z0+34, 80 bytes from x0+XH-4 rounded down to
+// step kernel tile: 60 x TZ cells worked by 64 x 4 threads per warp pair
+// (stress on 64 columns = tile + 2-cell halo each side); TZ = 32 for every
+// variant, PAL_TZ_SMALL = 16 for the FAST single-model ones.  TMA boxes of
+// 68 x TZ+8 (velocity) and 68 x TZ+4 (stress state) floats
+constexpr int PAL_TX = 60, PAL_TZ = 32, PAL_TZ_SMALL = 16;
+constexpr int TMA_VW = PAL_TX + 8;
+constexpr int tile_vh(int tz) { return tz + 8; }
+constexpr int tile_sh(int tz) { return tz + 4; }
+// material-id box: rows z0-2 .. z0+TZ+2, 80 bytes from x0+XH-4 rounded down to
 // 16 bytes (a TMA box starts on a 16-byte column), covering x0-4 .. x0+63
-constexpr int PAL_IDS_W = 80, PAL_IDS_H = PAL_TZ + 5;
+constexpr int PAL_IDS_W = 80;
+constexpr int tile_ids_h(int tz) { return tz + 5; }
 int launch_derive(const ModelDev &m, const StreamShot *shots_dev, int shot, int64_t n, float *out, void *stream);
 // allocation-free read-out of one derived field (sigma_xx 0, sigma_zz 1, p 2)
 // through the library's static scratch plane; returns a cudaError_t

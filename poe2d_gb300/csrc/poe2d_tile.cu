@@ -34,9 +34,14 @@ int step_mode(int sm, const ModelDev &m, const ModelDev *models, const StreamSho
 }  // namespace
 
 int launch_tile_step(const ModelDev &m, const StreamShot *shots_dev, int nshots, const int4 *items, int nitems, int k,
-                     int nk, bool exact, bool kone, int *queue, void *stream)
+                     int nk, bool exact, bool kone, int tile_z, int *queue, void *stream)
 {
     (void)nshots;
+    if (tile_z == PAL_TZ_SMALL) {
+        if (exact) return (int)cudaErrorInvalidValue;   // built for FAST stencils only
+        return tile_step_fast16(m, shots_dev, items, nitems, k, nk, kone, m.ids == nullptr, queue, stream);
+    }
+    if (tile_z != PAL_TZ) return (int)cudaErrorInvalidValue;
     return step_mode(stencil_mode(exact, m.qx.few_bits && m.qz.few_bits), m, nullptr, shots_dev, items, nitems, k,
                      nk, kone, m.ids == nullptr, queue, stream);
 }

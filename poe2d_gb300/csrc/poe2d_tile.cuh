@@ -135,34 +135,51 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0,
 // the other's work, measured 20 % slower: each group then waits for its own
 // buffer's copies.)  Buffers are handed over with mbarriers (full: producer
 // -> compute, empty: compute -> producer); every wait is bounded.
-constexpr int PCT = 576;                           // compute threads: 18 warps
 constexpr int ROWS = 4;                            // consecutive rows per compute task
-constexpr int PNT = PCT + 32;                      // + the producer warp
-constexpr int QX = PAL_TX, QZ = PAL_TZ;            // 60 x 32 output cells
-constexpr int IW = PAL_IDS_W, IH = PAL_IDS_H;      // ids: rows z0-2 .. z0+34; column x0-4 at (x0 & 15)
-constexpr int PV_FLOATS = TMA_VW * TMA_VH;         // 68 x 40
-constexpr int PS_BOX = TMA_VW * TMA_SH;            // 68 x 36 delivered per state plane
-constexpr int PS_FLOATS = PS_BOX;                  // slot stride: the 5 slots are one dense TMA box
-constexpr int PXW = TMA_VW, PZH = TMA_VH;          // profile slices: x0-4 .. x0+63, z0-4 .. z0+35
-constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
-constexpr int BUF_OFF_I = (BUF_OFF_S + 5 * PS_FLOATS * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
-constexpr int BUF_OFF_PZ = BUF_OFF_PX + (6 * PXW * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
-constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
-constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
-constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
-constexpr int PAL_OFF_B = 2 * BUF_BYTES;           // mbarriers and counters
-constexpr int PAL_OFF_R = PAL_OFF_B + 64;          // MS: the producer -> publisher ring
-constexpr int RING = 4;                            // ring slots
-constexpr size_t PAL_SMEM = PAL_OFF_R + 128;
-// every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
-constexpr uint32_t PAL_TX_BYTES = 4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
-static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
-static_assert(BUF_OFF_PX % 128 == 0 && BUF_OFF_PZ % 128 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
-              "TMA and bulk-copy destinations");
-static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 16 == 0 && IW >= 12 + 4 + 64 && PAL_SMEM <= 232448,
-              "16-byte box rows; the id box covers x0-4 .. x0+63 from any 16-byte start; shared memory budget");
+constexpr int QX = PAL_TX;                         // 60 output columns
+constexpr int IW = PAL_IDS_W;                      // ids: column x0-4 at (x0 & 15)
+constexpr int PXW = TMA_VW;                        // x profile slice: x0-4 .. x0+63
+constexpr int RING = 4;                            // MS: producer -> publisher ring slots
+// The geometry of a tile of TZ rows (60 x 32: every variant; 60 x 16: the
+// FAST single-model variants).  Shared memory per buffer: the 4 velocity
+// planes (68 x TZ+8), the 5 state planes (68 x TZ+4), the material ids
+// (80 x TZ+5 bytes), the two profile slices (6 x 68 and 6 x TZ+8 floats), a
+// material table, the item's parameters and (batch) its model descriptor.
+template <int TZ>
+struct Geo {
+    static constexpr int QZ = TZ;                              // output rows
+    static constexpr int NST = 2 * ((QZ + 4) / ROWS);          // stress tasks: (TZ+4)/4 bands x 2 halves
+    static constexpr int NVT = 2 * (QZ / ROWS);                // velocity tasks: TZ/4 bands x 2 halves
+    static constexpr int PCT = 32 * NST;                       // compute threads: one stress task per warp
+    static constexpr int PNT = PCT + 32;                       // + the producer warp
+    static constexpr int IH = TZ + 5;                          // id rows z0-2 .. z0+TZ+2
+    static constexpr int PV_FLOATS = TMA_VW * (TZ + 8);        // per velocity plane
+    static constexpr int PS_BOX = TMA_VW * (TZ + 4);           // delivered per state plane
+    static constexpr int PS_FLOATS = PS_BOX;                   // slot stride: the 5 slots are one dense TMA box
+    static constexpr int PZH = TZ + 8;                         // z profile slice: z0-4 .. z0+TZ+3
+    static constexpr int BUF_OFF_S = 4 * PV_FLOATS * 4;
+    static constexpr int BUF_OFF_I = (BUF_OFF_S + 5 * PS_FLOATS * 4 + 127) / 128 * 128;
+    static constexpr int BUF_OFF_PX = BUF_OFF_I + (IW * IH + 127) / 128 * 128;
+    static constexpr int BUF_OFF_PZ = BUF_OFF_PX + (6 * PXW * 4 + 127) / 128 * 128;
+    static constexpr int BUF_OFF_T = BUF_OFF_PZ + (6 * PZH * 4 + 127) / 128 * 128;
+    static constexpr int BUF_OFF_M = BUF_OFF_T + MAX_PALETTE * MT_W * 4;
+    static constexpr int BUF_OFF_MD = BUF_OFF_M + 128;
+    static constexpr int BUF_BYTES = (BUF_OFF_MD + (int)sizeof(ModelDev) + 127) / 128 * 128;
+    static constexpr int PAL_OFF_B = 2 * BUF_BYTES;            // mbarriers and counters
+    static constexpr int PAL_OFF_R = PAL_OFF_B + 64;           // MS: the producer -> publisher ring
+    static constexpr size_t PAL_SMEM = PAL_OFF_R + 128;
+    // every box arrives whole (out-of-range parts zero-filled): 9 state boxes, ids, profile slices
+    static constexpr uint32_t PAL_TX_BYTES =
+        4 * PV_FLOATS * 4 + 5 * PS_BOX * 4 + IW * IH + 6 * PXW * 4 + 6 * PZH * 4;
+    static_assert((QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && NST > NVT, "task grid");
+    static_assert(PV_FLOATS == TMA_VW * tile_vh(TZ) && PS_BOX == TMA_VW * tile_sh(TZ) && IH == tile_ids_h(TZ),
+                  "the boxes the host encodes");
+    static_assert(BUF_OFF_S % 128 == 0 && BUF_OFF_I % 128 == 0 && BUF_BYTES % 128 == 0, "TMA smem alignment");
+    static_assert(BUF_OFF_PX % 128 == 0 && BUF_OFF_PZ % 128 == 0 && BUF_OFF_T % 16 == 0 && BUF_OFF_MD % 16 == 0,
+                  "TMA and bulk-copy destinations");
+    static_assert(PXW % 4 == 0 && PZH % 4 == 0 && IW % 16 == 0 && IW >= 12 + 4 + 64 && PAL_SMEM <= 232448,
+                  "16-byte box rows; the id box covers x0-4 .. x0+63 from any 16-byte start; shared memory budget");
+};
 // state slots in shared memory; after the stress phase they hold its outputs
 // (the planes SF_SXZ .. SF_XI2 in order: one TMA box of depth 5 fills them)
 enum { PS_SXZ = 0, PS_G11, PS_G22, PS_XI1, PS_XI2 };
@@ -170,10 +187,6 @@ static_assert(SF_VX + 1 == SF_VZ && SF_VZ + 1 == SF_WX && SF_WX + 1 == SF_WZ && 
                   SF_G11 + 1 == SF_G22 && SF_G22 + 1 == SF_XI1 && SF_XI1 + 1 == SF_XI2,
               "velocity planes and stress-state planes are consecutive in the state array");
 enum { PO_SXX = PS_G11, PO_SZZ = PS_G22, PO_P = PS_XI1, PO_SXZ = PS_SXZ };
-// warp tasks per phase
-constexpr int NST = 2 * ((QZ + 4) / ROWS);         // stress: 9 bands x 2 halves
-constexpr int NVT = 2 * (QZ / ROWS);               // velocity: 8 bands x 2 halves
-static_assert((QZ + 4) % ROWS == 0 && QZ % ROWS == 0 && PCT == 32 * NST, "task grid");
 
 // Global accesses through the pointers the producer resolved for an item
 // (read back from shared memory, so the compiler sees generic pointers):
@@ -281,9 +294,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 // orders this thread's generic-proxy shared-memory accesses before later
 // async-proxy (TMA) writes to the same buffer
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// barrier 1: every compute warp
-__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(PCT) : "memory"); }
+// barrier 1: every compute warp (NT compute threads)
+template <int NT>
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory"); }
 // the same barrier, returning whether v held in every compute thread
+template <int NT>
 __device__ __forceinline__ bool compute_sync_and(bool v)
 {
     uint32_t r;
@@ -293,7 +308,7 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
         "bar.red.and.pred q, 1, %2, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)v), "n"(PCT)
+        : "r"((uint32_t)v), "n"(NT)
         : "memory");
     return r != 0;
 }
@@ -318,12 +333,22 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 // earlier steps, which every CTA finishes before it moves on, so the waits
 // cannot close a cycle; the producer keeps publishing its own finished items
 // while it waits.  Without MS (nk = 1) no tile waits for another.
-template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
-__global__ void __launch_bounds__(MS ? tile::PNT + 32 : tile::PNT, 1)
+template <int SM, bool KONE, bool MULTI, bool COEF, bool MS, int TZ>
+__global__ void __launch_bounds__(tile::Geo<TZ>::PNT + (MS ? 32 : 0), 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
            const int4 *__restrict__ items, int nitems, int k, int nk, int prefetch, int *__restrict__ queue)
 {
     using namespace tile;
+    using G = Geo<TZ>;
+    constexpr int QZ = G::QZ, NST = G::NST, NVT = G::NVT, PCT = G::PCT, IH = G::IH;
+    constexpr int PV_FLOATS = G::PV_FLOATS, PS_BOX = G::PS_BOX, PS_FLOATS = G::PS_FLOATS, PZH = G::PZH;
+    constexpr int BUF_OFF_S = G::BUF_OFF_S, BUF_OFF_I = G::BUF_OFF_I, BUF_OFF_PX = G::BUF_OFF_PX;
+    constexpr int BUF_OFF_PZ = G::BUF_OFF_PZ, BUF_OFF_T = G::BUF_OFF_T, BUF_OFF_M = G::BUF_OFF_M;
+    constexpr int BUF_OFF_MD = G::BUF_OFF_MD, BUF_BYTES = G::BUF_BYTES;
+    constexpr int PAL_OFF_B = G::PAL_OFF_B, PAL_OFF_R = G::PAL_OFF_R;
+    constexpr uint32_t PAL_TX_BYTES = G::PAL_TX_BYTES;
+    (void)PS_BOX;
+    (void)IH;
     constexpr bool EXACT = SM != SM_FAST;
     constexpr int NW = PCT / 32;             // compute warps: one stress task each
     static_assert(NST == NW && NW > NVT, "one stress task per warp; velocity warps, then receiver warps");
@@ -600,7 +625,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         // single model: one material table for every item, in buffer 0's slot
         float *t0 = reinterpret_cast<float *>(smp + BUF_OFF_T);
         for (int i = tid; i < mp.nmat * MT_W; i += PCT) t0[i] = mp.mtab[i];
-        compute_sync();
+        compute_sync<PCT>();
     }
     for (int j = 0;; ++j) {
         const int b = j & 1;
@@ -610,7 +635,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
         // parameters included) untrusted: touch nothing, join the item's
         // mid-point barrier, which then ends every compute thread together.
         if (!mbar_wait(&full[b], (uint32_t)((j >> 1) & 1))) {
-            compute_sync_and(false);
+            compute_sync_and<PCT>(false);
             if (tid == 0) atomicExch(err0(), 1);
             return;
         }
@@ -843,7 +868,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 }
             }
             if (!MULTI) prefetch_velocity_memory();
-            if (!compute_sync_and(true)) return false;   // false: a thread's wait for this item gave up
+            if (!compute_sync_and<PCT>(true)) return false;   // false: a thread's wait for this item gave up
 
             if (wid >= NVT) {
                 // ---- receivers of this tile (vx, vz before the update; p of this step)
@@ -1016,19 +1041,20 @@ inline int prefetch_strips(int nitems) { return nitems >= 8 * sm_count() ? 1 : 0
 
 // one launch of the step kernel of stencil mode SM: a single model (models
 // null) or a batch (models: device array; m unused)
-template <int SM, bool KONE, bool MULTI, bool COEF, bool MS>
+template <int SM, bool KONE, bool MULTI, bool COEF, bool MS, int TZ>
 int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items, int nitems,
                 int k, int nk, int *queue, cudaStream_t st)
 {
+    using G = tile::Geo<TZ>;
     static std::atomic<uint64_t> done{0};
-    auto kern = k_tile_pal<SM, KONE, MULTI, COEF, MS>;
-    smem_attr_once(kern, (int)tile::PAL_SMEM, done);
+    auto kern = k_tile_pal<SM, KONE, MULTI, COEF, MS, TZ>;
+    smem_attr_once(kern, (int)G::PAL_SMEM, done);
     const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
     if (grid <= 0) return (int)cudaGetLastError();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(MS ? tile::PNT + 32 : tile::PNT);   // MS: + the publisher warp
-    cfg.dynamicSmemBytes = tile::PAL_SMEM;
+    cfg.blockDim = dim3(G::PNT + (MS ? 32 : 0));   // MS: + the publisher warp
+    cfg.dynamicSmemBytes = G::PAL_SMEM;
     cfg.stream = st;
     // a step-spanning launch's CTAs wait for one another's tiles: a
     // cooperative launch guarantees that all of them are resident at once
@@ -1041,15 +1067,18 @@ int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *sho
                                    prefetch_strips(nitems), queue);
 }
 
-// every (KONE, MULTI, COEF, step-spanning) variant of one stencil mode
-template <int SM>
+// every (KONE, MULTI, COEF, step-spanning) variant of one stencil mode and
+// tile height (MULTI: batches, built for 32-row tiles only)
+template <int SM, int TZ>
 int tile_launch_mode(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
                      int nitems, int k, int nk, bool kone, bool coef, int *queue, cudaStream_t st)
 {
     const bool multi = models != nullptr;
+    if (multi && TZ != PAL_TZ) return (int)cudaErrorInvalidValue;
+    constexpr bool MU_OK = TZ == PAL_TZ;   // batch variants exist for the 32-row tile
     switch ((kone ? 8 : 0) | (multi ? 4 : 0) | (coef ? 2 : 0) | (nk > 1 ? 1 : 0)) {
 #define POE_TILE_CASE(s, KO, MU, CO, MS) \
-    case s: return tile_launch<SM, KO, MU, CO, MS>(m, models, shots, items, nitems, k, nk, queue, st);
+    case s: return tile_launch<SM, KO, MU && MU_OK, CO, MS, TZ>(m, models, shots, items, nitems, k, nk, queue, st);
         POE_TILE_CASE(0, false, false, false, false) POE_TILE_CASE(1, false, false, false, true)
         POE_TILE_CASE(2, false, false, true, false) POE_TILE_CASE(3, false, false, true, true)
         POE_TILE_CASE(4, false, true, false, false) POE_TILE_CASE(5, false, true, false, true)

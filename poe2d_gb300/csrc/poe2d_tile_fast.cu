@@ -7,7 +7,7 @@ namespace poe {
 int tile_step_fast(const ModelDev &m, const ModelDev *models, const StreamShot *shots, const int4 *items,
                    int nitems, int k, int nk, bool kone, bool coef, int *queue, void *stream)
 {
-    return tile_launch_mode<SM_FAST>(m, models, shots, items, nitems, k, nk, kone, coef, queue, (cudaStream_t)stream);
+    return tile_launch_mode<SM_FAST, PAL_TZ>(m, models, shots, items, nitems, k, nk, kone, coef, queue, (cudaStream_t)stream);
 }
 
 }  // namespace poe

@@ -244,10 +244,22 @@ class Solver:
         a step holds at most 96 tiles per SM."""
         self._check(L.lib().poe_tune_span(self.h, int(span)))
 
+    def tune_tile(self, tile_z):
+        """The step kernel's tile height: 32 (default) or 16 (FAST stencils, outside a batch)."""
+        self._check(L.lib().poe_tune_tile(self.h, int(tile_z)))
+
+    def tuning(self):
+        """The current tuning: dict(order, graph_steps, span, tile_z)."""
+        v = [C.c_int32(0) for _ in range(4)]
+        self._check(L.lib().poe_tuning(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("order", "graph_steps", "span", "tile_z"), (x.value for x in v)))
+
     def autotune(self, trial_steps=128):
-        """Time the 16 (order, graph_steps, span) candidates, keep the fastest; shots must
-        be at step 0 and are reset after.  Returns (order, graph_steps, ms per candidate),
-        candidate c = order c // 4, graph_steps (16, 64)[(c // 2) % 2], span c % 2."""
+        """Time the 32 (tile height, order, graph_steps, span) candidates, keep the fastest;
+        shots must be at step 0 and are reset after.  Returns (order, graph_steps, ms per
+        candidate), candidate c = tile height (32, 16)[c // 16], order (c // 4) % 4,
+        graph_steps (16, 64)[(c // 2) % 2], span c % 2 (ms -1: not a candidate for this
+        context); tuning() reports the winner's tile height."""
         o, g = C.c_int32(0), C.c_int32(0)
         ms = np.zeros(L.AUTOTUNE_CANDIDATES, np.float32)
         self._check(L.lib().poe_autotune(self.h, int(trial_steps), C.byref(o), C.byref(g), _f(ms)))

@@ -107,7 +107,7 @@ def test_constants_match_python(header_facts):
     # Solver.tune documents 0 rows, 1 columns, 2 tile-major, 3 balanced
     assert (L.ORDER_ROWS, L.ORDER_COLUMNS, L.ORDER_TILE_MAJOR, L.ORDER_BALANCED) == (
         c["POE_ORDER_ROWS"], c["POE_ORDER_COLUMNS"], c["POE_ORDER_TILE_MAJOR"], c["POE_ORDER_BALANCED"]) == (0, 1, 2, 3)
-    assert L.AUTOTUNE_CANDIDATES == c["POE_AUTOTUNE_CANDIDATES"] == 4 * 2 * 2
+    assert L.AUTOTUNE_CANDIDATES == c["POE_AUTOTUNE_CANDIDATES"] == 2 * 4 * 2 * 2
     assert (L.SPAN_NEVER, L.SPAN_ALWAYS, L.SPAN_AUTO) == (
         c["POE_SPAN_NEVER"], c["POE_SPAN_ALWAYS"], c["POE_SPAN_AUTO"]) == (0, 1, 2)
     assert L.CHECKPOINT_VERSION == c["POE_CHECKPOINT_VERSION"]

@@ -1,7 +1,7 @@
-"""The autotuner times the work-list orders, graph lengths and step-spanning
-launches on the context itself, keeps the fastest, and leaves the shots at
-step 0; whatever it picks, the results equal the default configuration's bit
-for bit."""
+"""The autotuner times the tile heights, work-list orders, graph lengths and
+step-spanning launches on the context itself, keeps the fastest, and leaves
+the shots at step 0; whatever it picks, the results equal the default
+configuration's bit for bit."""
 import numpy as np
 import pytest
 
@@ -30,12 +30,15 @@ def _run(poe, m, tune):
             s.add_shot(src, rec)
         picked = None
         if tune == "auto":
-            picked = s.autotune(32)
+            picked = s.autotune(32) + (s.tuning(),)
             assert all(s.steps(k) == 0 for k in range(len(srcs)))
         elif tune is not None:
             s.tune(*tune[:2])
             if len(tune) > 2:
                 s.tune_span(tune[2])
+            if len(tune) > 3:
+                s.tune_tile(tune[3])
+            assert s.tuning() == dict(zip(("order", "graph_steps", "span", "tile_z"), tune + (2, 32)[len(tune) - 2:]))
         s.run(150)
         return [s.traces(k) for k in range(len(srcs))] + [s.field("vz", 2)], picked
 
@@ -43,12 +46,16 @@ def _run(poe, m, tune):
 def test_autotune_keeps_results_and_reports_timings(poe):
     m = _model(poe)
     ref, _ = _run(poe, m, None)
-    got, (order, gsteps, ms) = _run(poe, m, "auto")
-    assert order in (0, 1, 2, 3) and gsteps in (16, 64) and ms.shape == (16,)
-    assert np.all(ms > 0) and ms.argmin() // 2 == 2 * order + (1 if gsteps == 64 else 0)
+    got, (order, gsteps, ms, tuning) = _run(poe, m, "auto")
+    assert order in (0, 1, 2, 3) and gsteps in (16, 64) and ms.shape == (32,)
+    assert np.all(ms > 0)                     # FAST, no batch: every candidate runs, 16-row tiles too
+    c = int(ms.argmin())
+    assert ((c // 4) % 4, (16, 64)[(c // 2) % 2], c % 2, (32, 16)[c // 16]) == (
+        order, gsteps, tuning["span"], tuning["tile_z"]) and tuning["order"] == order
     for a, b in zip(ref, got):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
-    for tune in ((1, 16, 0), (2, 64, 1), (3, 64, 0), (3, 16, 1), (0, 64, 0)):
+    for tune in ((1, 16, 0), (2, 64, 1), (3, 64, 0, 16), (3, 16, 1, 16), (0, 64, 0), (0, 64, 1, 16),
+                 (2, 16, 2, 16)):
         other, _ = _run(poe, m, tune)
         for a, b in zip(ref, other):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
@@ -64,6 +71,11 @@ def test_tuning_arguments_are_checked(poe):
             s.tune(0, 0)
         with pytest.raises(poe.PoeError):
             s.tune_span(3)
+        with pytest.raises(poe.PoeError):
+            s.tune_tile(24)
+        with pytest.raises(poe.PoeError):
+            s.tune_tile(16)                   # EXACT stencils: 32-row tiles only
+        assert s.tuning()["tile_z"] == 32
         s.run(5)
         with pytest.raises(poe.PoeError):
             s.autotune(8)                     # shots not at step 0
@@ -98,3 +110,54 @@ def test_span_auto_spans_steps_of_few_tiles_only(poe):
             s.run(128)
             s.sync()
             assert s.launches - n0 == 2 * per_graph, (nshots, span)
+
+
+@pytest.mark.parametrize("palette", [True, False])
+@pytest.mark.parametrize("kmax", [1.0, 1.5])
+def test_small_tiles_equal_large_tiles(poe, palette, kmax):
+    """60 x 16 tiles (FAST) end exactly where 60 x 32 tiles end, with and
+    without step-spanning launches, K = 1 or not, palette or coefficient
+    planes, through graphs, direct tails, a reset and a restored checkpoint;
+    the batch takes 32-row contexts only."""
+    g, coef, px, pz, rec, srcs = _model(poe)
+    par = poe.pml_defaults(15, 200.0, 3000.0)
+    par.k_max = kmax
+    px, pz = poe.pml_profiles(g, params=par)
+    out = []
+    for tile, span in ((32, 0), (16, 0), (16, 1)):
+        with poe.Solver(g, coef, px, pz, fast=True, palette=palette) as s:
+            for src in srcs[:2]:
+                s.add_shot(src, rec)
+            s.tune_tile(tile)
+            s.tune_span(span)
+            s.run(150)
+            img = s.checkpoint(1)
+            s.run(40)
+            s.reset_shot(0)
+            s.run(70)
+            s.restore(img, 1)
+            s.run(33)
+            out.append([(s.traces(k), s.field("vz", k), s.field("p", k), s.field("xi1", k)) for k in range(2)])
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            for x, y in zip(a, b):
+                assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_batch_takes_large_tiles_only(poe):
+    g, coef, px, pz, rec, srcs = _model(poe)
+    a = poe.Solver(g, coef, px, pz, fast=True)
+    b = poe.Solver(g, coef, px, pz, fast=True)
+    for s in (a, b):
+        s.add_shot(srcs[0], rec)
+    a.tune_tile(16)
+    with pytest.raises(poe.PoeError):
+        poe.Batch([a, b])
+    a.tune_tile(32)
+    with poe.Batch([a, b]) as bt:
+        with pytest.raises(poe.PoeError):
+            b.tune_tile(16)                   # a batch member
+        bt.run([10, 10])
+        bt.sync()
+    for s in (a, b):
+        s.close()

@@ -1,9 +1,11 @@
 """Register and local-memory use of every kernel, from ptxas's own report
 (``-Xptxas -v``, kept by the build in ``poe2d_gb300/_build/*.ptxas.txt``).
 
-The step kernel runs 608 threads per CTA (18 compute warps + 1 producer;
-640 with the step-spanning variants' publisher warp) at one CTA per SM, so
-ptxas caps it at 96 registers; what does not fit goes to local memory.  The single-model variants and the batch variants the batched
+The step kernel runs 608 threads per CTA on 60 x 32 tiles (18 compute warps
++ 1 producer; 640 with the step-spanning variants' publisher warp) at one CTA
+per SM, so ptxas caps it at 96 registers; what does not fit goes to local
+memory.  The 60 x 16 variants (FAST, single model) run 10 compute warps and
+may take 128.  The single-model variants and the batch variants the batched
 benchmarks run (palette models with K = 1, FAST or few-bit EXACT stencils)
 must not spill.  The remaining batch variants (K != 1, per-cell
 coefficients, or EXACT at a spacing whose 24 h needs more than 8 bits) spill
@@ -53,31 +55,33 @@ def reports():
     return got
 
 
-TILE_UNITS = ("poe2d_tile_fast.cu", "poe2d_tile_exact.cu", "poe2d_tile_exact_any.cu")
+TILE_UNITS = ("poe2d_tile_fast.cu", "poe2d_tile_exact.cu", "poe2d_tile_exact_any.cu", "poe2d_tile_fast16.cu")
 
 
 def _step_variants(reports):
     out = {}
     for unit in TILE_UNITS:
         for name, res in reports[unit].items():
-            m = re.search(r"k_tile_palILi(\d)ELb(\d)ELb(\d)ELb(\d)ELb(\d)E", name)
+            m = re.search(r"k_tile_palILi(\d)ELb(\d)ELb(\d)ELb(\d)ELb(\d)ELi(\d+)E", name)
             if m:
-                sm, kone, multi, coef, span = (int(v) for v in m.groups())
-                out[(MODES[sm], bool(kone), bool(multi), bool(coef), bool(span))] = res
+                sm, kone, multi, coef, span, tz = (int(v) for v in m.groups())
+                out[(MODES[sm], bool(kone), bool(multi), bool(coef), bool(span), tz)] = res
     return out
 
 
 def test_every_step_kernel_variant_is_built(reports):
     v = _step_variants(reports)
-    assert len(v) == 3 * 2 * 2 * 2 * 2, sorted(v)
+    assert len([k for k in v if k[5] == 32]) == 3 * 2 * 2 * 2 * 2, sorted(v)
+    small = sorted(k for k in v if k[5] == 16)
+    assert len(small) == 2 * 2 * 2 and all(k[0] == "FAST" and not k[2] for k in small), small
     for key, (regs, _, _, _) in v.items():
-        assert regs <= 96, (key, regs)   # 608 (640) threads at one CTA per SM
+        assert regs <= (96 if key[5] == 32 else 128), (key, regs)   # threads at one CTA per SM
 
 
 def test_single_model_and_benchmarked_batch_variants_do_not_spill(reports):
     v = _step_variants(reports)
     for key, (regs, stack, st, ld) in v.items():
-        mode, kone, multi, coef, span = key
+        mode, kone, multi, coef, span, tz = key
         benchmarked_batch = multi and kone and not coef and mode in ("FAST", "EXACT_FEW")
         if not multi or benchmarked_batch:
             assert st == 0 and ld == 0, (key, st, ld)
