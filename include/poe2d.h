@@ -219,12 +219,15 @@ int poe_get_derived_noalloc(poe_ctx *ctx, int32_t shot, int32_t field, float *ho
 
 /* The kernels' bounded waits, checked: no reference counterpart.  Every wait
  * of a kernel on an mbarrier (a tile's copies landing, a buffer's release)
- * polls a bounded number of times; a wait that gives up flags the context's
- * error (POE_ETIMEOUT from the next call that checks it) and the kernel ends,
- * so a lost arrival cannot hang the GPU.  This runs that wait on device
- * `device` against a barrier no thread arrives at, for at most `polls` polls
- * (1 .. 2^24): *gave_up = 1 when the wait ended at its limit (the expected
- * answer), and the device stays usable afterwards. */
+ * or on other tiles' flags (a step-spanning launch) polls a bounded number of
+ * times; a wait that gives up flags the context's error (POE_ETIMEOUT from the
+ * next call that checks it) and the kernel ends, so a lost arrival or flag
+ * cannot hang the GPU.  This runs the step kernel's wait code on device
+ * `device` against a barrier no thread arrives at and against a tile flag
+ * nothing sets, for at most `polls` polls each (1 .. 2^24), and the flag wait
+ * once more against flags that are set: *gave_up = 1 when the first two
+ * ended at their limit and the third passed (the expected answer), and the
+ * device stays usable afterwards. */
 int poe_wait_limit_check(int32_t device, int32_t polls, int32_t *gave_up);
 
 /* Overwrite one full field of a shot (checkpoint restore; no reference counterpart). */

@@ -911,15 +911,17 @@ int poe_wait_limit_check(int32_t device, int32_t polls, int32_t *gave_up)
 {
     if (!gave_up || polls < 1 || polls > (1 << 24)) return POE_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return POE_ECUDA;
-    int *err = nullptr;
+    int *buf = nullptr;   // [0]: error bits; [1..9]: tile flags
     int flag = 0;
-    cudaError_t e = cudaMalloc(&err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
-    if (e == cudaSuccess) e = (cudaError_t)launch_wait_limit(err, polls, nullptr);
-    if (e == cudaSuccess) e = cudaMemcpy(&flag, err, sizeof(int), cudaMemcpyDeviceToHost);
-    cudaFree(err);
+    const int h[10] = {0, 0, 5, 5, 5, 5, 5, 5, 5, 5};
+    cudaError_t e = cudaMalloc(&buf, sizeof(h));
+    if (e == cudaSuccess) e = cudaMemcpy(buf, h, sizeof(h), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = (cudaError_t)launch_wait_limit(buf, buf + 1, polls, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, buf, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
     if (e != cudaSuccess) return POE_ECUDA;
-    *gave_up = flag;
+    // both waits on conditions that never hold gave up, the one on set flags did not
+    *gave_up = flag == 3 ? 1 : 0;
     return POE_OK;
 }
 

@@ -134,9 +134,11 @@ int tile_step_fast16(const ModelDev &m, const StreamShot *shots, const int4 *ite
                      bool kone, bool coef, int *queue, void *stream);
 // *shots[i].step += by for i < nshots
 int launch_advance_shots(const StreamShot *shots_dev, int nshots, int64_t by, void *stream);
-// one thread waits, polls times at most, on an mbarrier no thread arrives at;
-// sets *err when the wait gives up
-int launch_wait_limit(int *err, int polls, void *stream);
+// the step kernel's bounded waits against conditions that never hold: an
+// mbarrier no thread arrives at (bit 0 of *err when it gives up), a tile flag
+// nothing sets (bit 1), and flags that are set (bit 2 if that wait gives up);
+// flags: 9 device ints, flags[0] = 0, flags[1..8] = 5
+int launch_wait_limit(int *err, const int *flags, int polls, void *stream);
 // step kernel tile: 60 x TZ cells worked by 64 x 4 threads per warp pair
 // (stress on 64 columns = tile + 2-cell halo each side); TZ = 32 for every
 // variant, PAL_TZ_SMALL = 16 for the FAST single-model ones.  TMA boxes of

@@ -54,22 +54,29 @@ int launch_batch_step(const ModelDev *models_dev, const StreamShot *shots_dev, c
                      queue, stream);
 }
 
-// the bounded wait on a phase that never completes (no thread arrives): the
-// waiting thread gives up after `polls` polls, flags the error and returns
-__global__ void k_wait_limit(int *err, int polls)
+// the step kernel's bounded waits, on the GPU: (1) an mbarrier phase that
+// never completes (no thread arrives), (2) tile flags one of which nothing
+// sets (flags[0] = 0; flags[1..8] hold 5), (3) the same flags with the unset
+// one not watched, which must pass.  err: bit 0 and bit 1 when waits (1) and
+// (2) gave up after `polls` polls, bit 2 if wait (3) did
+__global__ void k_wait_limit(int *err, const int *flags, int polls)
 {
     __shared__ uint64_t bar;
-    if (threadIdx.x == 0) {
+    const int lane = threadIdx.x;
+    if (lane == 0) {
         mbar_init(&bar, 1);
         mbar_fence_init();
     }
     __syncthreads();
-    if (threadIdx.x == 0 && !mbar_wait_n(&bar, 0, polls)) atomicExch(err, 1);
+    if (lane == 0 && !mbar_wait_n(&bar, 0, polls)) atomicOr(err, 1);
+    __syncwarp();
+    if (!tile::wait_flags(lane < 9 ? flags + lane : nullptr, 1, polls) && lane == 0) atomicOr(err, 2);
+    if (!tile::wait_flags(lane >= 1 && lane < 9 ? flags + lane : nullptr, 5, polls) && lane == 0) atomicOr(err, 4);
 }
 
-int launch_wait_limit(int *err, int polls, void *stream)
+int launch_wait_limit(int *err, const int *flags, int polls, void *stream)
 {
-    k_wait_limit<<<1, 32, 0, (cudaStream_t)stream>>>(err, polls);
+    k_wait_limit<<<1, 32, 0, (cudaStream_t)stream>>>(err, flags, polls);
     return (int)cudaGetLastError();
 }
 

@@ -248,6 +248,18 @@ __device__ __forceinline__ void st_release_cta(int *p, int v)
 {
     asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
 }
+// the warp waits until every lane's flag (a lane with a null flag watches
+// none) reads at least want, each lane polling its own with ld.acquire.gpu;
+// false when the flags still fall short after `polls` rounds (bounded)
+__device__ __forceinline__ bool wait_flags(const int *flag, int want, int polls)
+{
+    bool ok = flag == nullptr;
+    for (int poll = 0;; ++poll) {
+        if (!ok) ok = ld_acquire(flag) >= want;
+        if (__all_sync(0xffffffffu, ok)) return true;
+        if (poll >= polls) return false;
+    }
+}
 
 // new w and v of one cell from its coefficient planes (c at the cell, planes
 // pl apart), with the reference's float operations in its order (cu:293-311,
@@ -522,15 +534,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                 const int *flag = (kk > k && lane < 9 && ux >= 0 && ux < ntx && uz >= 0 && uz < ntz)
                                       ? S.done + uz * ntx + ux
                                       : nullptr;
-                bool ok = flag == nullptr;
-                for (int poll = 0;; ++poll) {
-                    if (!ok) ok = ld_acquire(flag) >= nn - 1;
-                    if (__all_sync(0xffffffffu, ok)) break;
-                    if (poll >= (1 << 20)) {
-                        gave_up = true;
-                        break;
-                    }
-                }
+                if (!wait_flags(flag, nn - 1, 1 << 20)) gave_up = true;
                 if (gave_up) {
                     if (lane == 0) atomicExch(mp.err ? mp.err : models[it.x].err, 1);
                     break;

@@ -141,8 +141,10 @@ def checkpoint_info(image):
 
 
 def wait_limit_check(polls=1000, device=0):
-    """Run the kernels' bounded mbarrier wait against a barrier nothing arrives
-    at (poe_wait_limit_check): True when the wait gave up at its limit."""
+    """Run the step kernel's bounded waits against a barrier nothing arrives at
+    and a tile flag nothing sets, and the flag wait against set flags
+    (poe_wait_limit_check): True when the first two gave up at their limit and
+    the third passed."""
     out = C.c_int32(0)
     check(L.lib().poe_wait_limit_check(int(device), int(polls), C.byref(out)))
     return out.value == 1

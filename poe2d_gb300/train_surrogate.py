@@ -156,8 +156,11 @@ def main(argv=None):
         spec_tr += D.uneven_specs(args.seed * 1000 + k, 256, args.side_min, args.side_max, args.gas_max, args.phi,
                                   args.f0)
     spec_tr = spec_tr[:args.train]
-    spec_ho = D.uneven_specs(args.seed * 1000 + 999, 256, args.side_min, args.side_max, args.gas_max, args.phi,
-                             args.f0)[:args.heldout]
+    spec_ho = []
+    for k in range(math.ceil(args.heldout / 256)):      # seeds counting down from 999: none a training seed
+        spec_ho += D.uneven_specs(args.seed * 1000 + 999 - k, 256, args.side_min, args.side_max, args.gas_max,
+                                  args.phi, args.f0)
+    spec_ho = spec_ho[:args.heldout]
     t0 = time.perf_counter()
     m_tr, s_tr, y_tr, ts_tr, c_tr = generate(spec_tr, stream)
     m_ho, s_ho, y_ho, ts_ho, c_ho = generate(spec_ho, stream)

@@ -1,13 +1,15 @@
-"""The kernels' waits are bounded: a wait whose phase never completes gives up,
-flags the error and ends its kernel, and the device stays usable (no GPU is
-hung or faulted: the barrier simply never receives an arrival)."""
+"""The kernels' waits are bounded: a wait whose phase never completes, or on a
+tile flag that nothing sets, gives up, flags the error and ends its kernel,
+and the device stays usable (no GPU is hung or faulted: the barrier simply
+never receives an arrival, the flag is never written); the same flag wait on
+flags that are set passes at once."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-def test_wait_on_a_barrier_nobody_arrives_at_gives_up(poe):
+def test_waits_on_a_barrier_nobody_arrives_at_and_a_flag_nobody_sets_give_up(poe):
     assert poe.wait_limit_check(polls=1000)
     assert poe.wait_limit_check(polls=1)
 
