@@ -1,10 +1,13 @@
-// poe2d_tile.cuh -- the fused time step: one launch = stress + velocity.
-// Included by one instantiation unit per stencil mode (poe2d_tile_fast.cu,
-// poe2d_tile_exact.cu, poe2d_tile_exact_any.cu), which compile in parallel.
+// poe2d_tile.cuh -- the fused time step: stress + velocity in one kernel, one
+// step per launch or (step-spanning) many.  Included by one instantiation
+// unit per stencil mode (poe2d_tile_fast.cu, poe2d_tile_exact.cu,
+// poe2d_tile_exact_any.cu) and by poe2d_tile_fast16.cu (FAST, 60 x 16 tiles),
+// which compile in parallel.
 //
-// k_tile_pal: a persistent, warp-specialised kernel (one CTA per SM) walks a
-// work list of 60 x 32 tiles of any number of shots (and, for batches, of
-// models).  Per tile: stress on the tile + 2-cell halo (64 x 36 cells):
+// k_tile_pal: a persistent, warp-specialised kernel (one CTA per SM) takes
+// 60 x 32 (or 60 x 16) tiles of any number of shots (and, for batches, of
+// models) from a work queue.  Per tile: stress on the tile + 2-cell halo
+// (64 x 36 cells for 32 rows):
 // strains, fluid content, sigma2 = p, sigma_xz, sigma_xx, sigma_zz (cu:49-112,
 // 202-229, 231-244) -> shared memory, the integrated state of the tile's own
 // cells -> HBM; the tile's receivers (before the velocity update, as
@@ -115,8 +118,8 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0,
 // 1/co, 1/c1) comes from a table row in shared memory; other models (COEF)
 // read the 8 coefficient planes per cell.
 //
-// Persistent, warp-specialised and double-buffered: one CTA per SM walks the
-// work list of (model, shot, tile) items.  A producer warp runs one item
+// Persistent, warp-specialised and double-buffered: one CTA per SM takes
+// (model, shot, tile) items from the work list.  A producer warp runs one item
 // ahead: it resolves the item's model and shot (a chain of dependent global
 // loads that would otherwise stall every warp at each item), writes the
 // item's parameters to shared memory, and fills the free buffer with five TMA
@@ -124,12 +127,12 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0,
 // each; the material ids; the two C-PML profile slices) and, for a batch item,
 // a bulk copy of its material table.  Each copy costs the producer about 120
 // cycles to issue, so the copies are few and large.  Eighteen compute warps
-// compute the items from the buffers: a warp task is 32 consecutive columns
-// (conflict-free shared-memory rows) of a band of 4 consecutive rows, so the
-// z-stencils of a column reuse the values of the rows before them in
-// registers.  Stress: 9 bands x 2 halves cover the 64 x 36 stress cells;
-// velocity: 8 bands x 2 halves cover the 60 x 32 tile, while the remaining
-// two warps record the tile's receivers.  The warps may run one item ahead
+// (ten for 16-row tiles) compute the items from the buffers: a warp task is
+// 32 consecutive columns (conflict-free shared-memory rows) of a band of 4
+// consecutive rows, so the z-stencils of a column reuse the values of the
+// rows before them in registers.  Stress: 9 bands x 2 halves cover the
+// 64 x 36 stress cells; velocity: 8 bands x 2 halves cover the 60 x 32 tile,
+// while the remaining two warps record the tile's receivers.  The warps may run one item ahead
 // of each other.  (Splitting them into two groups of 9 that each own one
 // buffer and alternate items, so that one group's mid-item barrier overlaps
 // the other's work, measured 20 % slower: each group then waits for its own
