@@ -683,12 +683,13 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
             auto addm = [](float v, float mv) { return (SM == SM_FAST && IN) ? v : v + mv; };
             // The velocity C-PML memory this thread updates in place after the
             // barrier (rows zb0 .. zb0+3 of column lx, on the strips), to L1.  A
-            // single model prefetches it just before the barrier, while the other
-            // warps finish their stress rows: prefetched at the tile start together
-            // with the stress phase's memory it overflows the L1 that the tile
-            // buffers leave (about 28 KB beside 205 KB of shared memory).  The
-            // batch kernel prefetches it at the tile start, where it spills no
-            // registers.
+            // single model's per-step launch prefetches it just before the
+            // barrier, while the other warps finish their stress rows: prefetched
+            // at the tile start together with the stress phase's memory it
+            // overflows the L1 that the tile buffers leave (about 28 KB beside
+            // 205 KB of shared memory).  The batch kernel prefetches it at the
+            // tile start, where it spills no registers, and so does a
+            // step-spanning launch, whose prefetches go to L2 (+0.3 %).
             auto prefetch_velocity_memory = [&]() {
                 if (IN || !prefetch || wid >= NVT || lx >= QX || x0 + lx > NX) return;
                 const int x = x0 + lx;
@@ -708,7 +709,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                             prefetch_m<MS>(IM.mzv + a * hzp + zr * P + x + XH);
                 }
             };
-            if (MULTI) prefetch_velocity_memory();
+            if (MULTI || MS) prefetch_velocity_memory();
             if (COEF && wid < NVT && lx < QX) {
                 // the density coefficients this thread's velocity rows read (rows
                 // zb0 .. zb0+4 of column lx): to L1 now, read after the stress phase
@@ -874,7 +875,7 @@ k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamS
                     ss[PO_SXZ * PS_FLOATS + so] = sxz;
                 }
             }
-            if (!MULTI) prefetch_velocity_memory();
+            if (!MULTI && !MS) prefetch_velocity_memory();
             if (!compute_sync_and<PCT>(true)) return false;   // false: a thread's wait for this item gave up
 
             if (wid >= NVT) {

@@ -9,7 +9,11 @@
 //   thread 32   MMA issuer: four tcgen05.mma (K = 16 each) per stage, then
 //               tcgen05.commit frees the stage; a last commit signals the end;
 //   warps 0-3   epilogue: each warp reads its 32 TMEM lanes (rows) with
-//               tcgen05.ld and applies alpha, bias, ReLU, the bf16/f32 stores.
+//               tcgen05.ld and applies alpha, bias, ReLU; a plain output
+//               (FP32 or bf16, not accumulated, one K split) is staged in the
+//               freed pipeline stages as 128-byte-swizzled 128 x 128-byte
+//               blocks and written by TMA tensor stores (coalesced whole
+//               rows, asynchronous), otherwise each thread stores its row.
 // K may be split over blockIdx.z (ksplit > 1): each split writes an FP32
 // partial tile to a workspace and a reduction kernel applies the epilogue in
 // a fixed order, so results do not depend on scheduling.
@@ -44,6 +48,7 @@ struct GemmSmem {
     static constexpr int A_BYTES = BM * BK * 2;             // 16 KB
     static constexpr int B_BYTES = BN * BK * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
+    static_assert(BM * BN * 4 <= STAGES * STAGE, "an FP32 output tile fits in the pipeline stages");
     static constexpr int BAR_OFF = STAGES * STAGE;
     static constexpr int BIAS_OFF = BAR_OFF + (2 * STAGES + 1) * 8 + 8;
     static constexpr int TOTAL = BIAS_OFF + BN * 4 + 1024;   // + alignment slack
@@ -51,10 +56,14 @@ struct GemmSmem {
     static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
 };
 
+// output through TMA stores: OUT_F32 (32-column blocks) or OUT_BF16 (64-column blocks)
+enum { OUT_THREADS = 0, OUT_F32 = 1, OUT_BF16 = 2 };
+
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(NT, 1)
-k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, int M, int N, int K,
-       int kblocks_per_split, Epilogue e, float *partial, int *err)
+k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
+       const __grid_constant__ CUtensorMap tC, int out_mode, int M, int N, int K, int kblocks_per_split, Epilogue e,
+       float *partial, int *err)
 {
     using L = GemmSmem<BN, STAGES>;
     extern __shared__ unsigned char smraw[];
@@ -171,6 +180,29 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
                 if (e.relu) t = fmaxf(t, 0.0f);
                 x[j] = t;
             }
+            if (out_mode != OUT_THREADS) {
+                // 128 x 128-byte block of this column range; 16-byte piece q of
+                // row r sits at piece q ^ (r & 7) (the 128-byte swizzle)
+                const int r = warp * 32 + lane, sw = r & 7;
+                if (out_mode == OUT_F32) {
+                    unsigned char *blk = sm + (c >> 1) * (BM * 128) + r * 128;
+    #pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<float4 *>(blk + ((((c & 1) * 4 + q) ^ sw) << 4)) =
+                            make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+                } else {
+                    unsigned char *blk = sm + (c >> 2) * (BM * 128) + r * 128;
+    #pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        uint4 w;
+                        __nv_bfloat162 *h2 = reinterpret_cast<__nv_bfloat162 *>(&w);
+    #pragma unroll
+                        for (int i = 0; i < 4; ++i) h2[i] = __floats2bfloat162_rn(x[8 * q + 2 * i], x[8 * q + 2 * i + 1]);
+                        *reinterpret_cast<uint4 *>(blk + ((((c & 3) * 2 + q) ^ sw) << 4)) = w;
+                    }
+                }
+                continue;
+            }
             const size_t o = (size_t)row * e.ldc + nb;
             if (e.out_f32) {
                 float *p = e.out_f32 + o;
@@ -211,6 +243,18 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
                         if (nb + j < N) p[j] = __float2bfloat16_rn(x[j]);
                 }
             }
+        }
+    }
+    if (out_mode != OUT_THREADS) {
+        // the staged tile, once every thread's part is in: TMA stores of its
+        // 128-byte column blocks (rows and columns past M, N are not written)
+        fence_proxy_async_smem();
+        const bool all_ok = __syncthreads_and(ok) != 0;
+        if (tid == 0 && all_ok && nkb > 0) {
+            const int cols = out_mode == OUT_F32 ? 32 : 64;   // columns per 128-byte block
+            for (int j = 0; j < BN / cols && n0 + j * cols < N; ++j) tma_store_2d(&tC, n0 + j * cols, m0, sm + j * (BM * 128));
+            bulk_commit();
+            bulk_wait_all();   // the stores have read the stage buffers and written the output
         }
     }
     tc_fence_before();
@@ -271,6 +315,22 @@ bool make_map(CUtensorMap *m, const void *base, int rows, int cols, int ld, int 
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the output C as the TMA store's tensor: N columns x M rows (pitch ldc
+// elements), 128 x 128-byte boxes, 128-byte swizzle
+bool make_out_map(CUtensorMap *m, void *base, bool f32, int rows, int cols, int ldc)
+{
+    EncodeFn fn = encode_fn();
+    if (!fn) return false;
+    const int es = f32 ? 4 : 2;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ldc * es};
+    const cuuint32_t box[2] = {(cuuint32_t)(128 / es), (cuuint32_t)BM};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int sm_count()
 {
     static int sms = 0;
@@ -284,14 +344,15 @@ int sm_count()
 }
 
 template <int BN, int ST>
-int launch(const CUtensorMap &ta, const CUtensorMap &tb, int M, int N, int K, int splits, int kper, const Epilogue &e,
-           float *ws, int *err, cudaStream_t st)
+int launch(const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tc, int out_mode, int M, int N, int K,
+           int splits, int kper, const Epilogue &e, float *ws, int *err, cudaStream_t st)
 {
     using L = GemmSmem<BN, ST>;
     static std::atomic<uint64_t> done{0};
     poe::smem_attr_once(k_gemm<BN, ST>, L::TOTAL, done);
     const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
-    k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, M, N, K, kper, e, splits > 1 ? ws : nullptr, err);
+    k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, tc, out_mode, M, N, K, kper, e, splits > 1 ? ws : nullptr,
+                                               err);
     return (int)cudaGetLastError();
 }
 }  // namespace
@@ -320,10 +381,23 @@ int gemm(const Gemm &g, const Epilogue &e, float *ws, int64_t ws_floats, int *er
     const int kper = (nkb + splits - 1) / splits;
     splits = (nkb + kper - 1) / kper;
     const bool short_k = kper <= 4;
-    int rc = BN == 128 ? (short_k ? launch<128, 2>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
-                                  : launch<128, 4>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st))
-                       : (short_k ? launch<64, 2>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st)
-                                  : launch<64, 4>(ta, tb, g.M, g.N, g.K, splits, kper, e, ws, err, st));
+    // one plain output (no accumulation, one K split, 16-byte rows and base):
+    // written by TMA stores from the stage buffers
+    CUtensorMap tc;
+    std::memset(&tc, 0, sizeof(tc));
+    int out_mode = OUT_THREADS;
+    if (splits == 1 && !e.accumulate && (e.out_f32 == nullptr) != (e.out_bf16 == nullptr)) {
+        const bool f32 = e.out_f32 != nullptr;
+        void *base = f32 ? (void *)e.out_f32 : (void *)e.out_bf16;
+        if ((e.ldc % (f32 ? 4 : 8)) == 0 && ((uintptr_t)base & 15) == 0 &&
+            make_out_map(&tc, base, f32, g.M, g.N, e.ldc))
+            out_mode = f32 ? OUT_F32 : OUT_BF16;
+    }
+    int rc = BN == 128
+                 ? (short_k ? launch<128, 2>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st)
+                            : launch<128, 4>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st))
+                 : (short_k ? launch<64, 2>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st)
+                            : launch<64, 4>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st));
     if (rc || splits == 1) return rc;
     const int64_t total = (int64_t)g.M * g.N;
     int blocks = (int)((total + 255) / 256);

@@ -56,6 +56,21 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0,
         : "memory");
 }
 
+// 2-D tiled TMA store of box (c0 inner, c1 outer) from shared memory, in the
+// thread's bulk async-group; parts of the box outside the tensor are not
+// written.  c0 * element size must be a multiple of 16; c0, c1 >= 0.
+__device__ __forceinline__ void tma_store_2d(const void *desc, int c0, int c1, const void *src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"(desc), "r"(c0), "r"(c1), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// every bulk store of this thread's groups has completed (its writes performed)
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// this thread's shared-memory writes, before later async-proxy (TMA) reads of them
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // ---- tcgen05 (one CTA, cta_group::1)
 
 // allocate ncols TMEM columns (power of two >= 32); the whole warp executes it

@@ -87,3 +87,34 @@ def test_gemm_rejects_bad_pitch(poe):
     st = lib.poe_sg_gemm(A.data_ptr(), 70, B.data_ptr(), 72, 64, 64, 64, 1.0, None, 0, out.data_ptr(), None, 64, 0,
                          None, 0, err.data_ptr(), None)
     assert st == 1
+
+
+@pytest.mark.parametrize("f32,M,N,ldc", [
+    (True, 300, 200, 208),     # TMA-store epilogue, a padded pitch: columns N.. ldc stay untouched
+    (True, 300, 200, 202),     # pitch not a multiple of 16 bytes: per-thread stores
+    (False, 300, 200, 200),    # bf16 through TMA stores, tails in both dimensions
+    (False, 1000, 48, 56),     # bf16, a 64-wide tile, padded pitch
+    (False, 300, 200, 204),    # bf16 pitch not a multiple of 16 bytes
+])
+def test_gemm_output_paths_and_pitches(poe, f32, M, N, ldc):
+    """Both epilogues (TMA stores of the staged tile, per-thread stores) write
+    exactly the M x N result and nothing past it in the row pitch."""
+    lib = poe.lib()
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N + ldc)
+    K = 192
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn(N, device="cuda", generator=g)
+    if f32:
+        buf = torch.full((M, ldc), 7.0, device="cuda")
+        _gemm(lib, A, B, 1.0, b, True, out32=buf)
+        got = buf[:, :N]
+        assert bool((buf[:, N:] == 7.0).all())
+    else:
+        buf = torch.full((M, ldc), 7.0, device="cuda").to(torch.bfloat16)
+        _gemm(lib, A, B, 1.0, b, True, out16=buf)
+        got = buf[:, :N].float()
+        assert bool((buf[:, N:].float() == 7.0).all())
+    ref = torch.relu(A.float() @ B.float().T + b)
+    tol = 1e-4 if f32 else 1e-2
+    assert float((got - ref).abs().max()) <= tol * float(ref.abs().max())
