@@ -59,11 +59,20 @@ struct GemmSmem {
 // output through TMA stores: OUT_F32 (32-column blocks) or OUT_BF16 (64-column blocks)
 enum { OUT_THREADS = 0, OUT_F32 = 1, OUT_BF16 = 2 };
 
+// A operand of a k = 3 time convolution read in place (T > 0): tA is the 3-D
+// map {cin, T, B} of x, k-block kk = 64 j of K = 3 cin reads tap kk / cin,
+// channels kk % cin, rows s + off[tap] of the tile's items; the output rows
+// are the phase's rows of the upsampled time axis (tC 3-D {N, up, M})
+struct ConvA {
+    int T = 0, cin = 0, up = 1, phase = 0;
+    int off[3] = {0, 0, 0};
+};
+
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(NT, 1)
 k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
-       const __grid_constant__ CUtensorMap tC, int out_mode, int M, int N, int K, int kblocks_per_split, Epilogue e,
-       float *partial, int *err)
+       const __grid_constant__ CUtensorMap tC, int out_mode, const ConvA ca, int M, int N, int K,
+       int kblocks_per_split, Epilogue e, float *partial, int *err)
 {
     using L = GemmSmem<BN, STAGES>;
     extern __shared__ unsigned char smraw[];
@@ -108,7 +117,16 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
             }
             unsigned char *a = sm + s * L::STAGE;
             mbar_expect_tx(&full[s], L::TX);
-            tma_load_2d(a, &tA, (kb0 + i) * BK, m0, &full[s]);
+            if (ca.T > 0) {
+                // the tile's 128 rows of x: one item's rows m0 % T .. +127 (T >= 128) or
+                // 128 / T whole items (T < 128), shifted by the tap's offset (rows
+                // outside an item arrive as zeros: the convolution's padding)
+                const int kk = (kb0 + i) * BK, tap = kk / ca.cin, b0 = m0 / ca.T;
+                const int off = tap == 0 ? ca.off[0] : (tap == 1 ? ca.off[1] : ca.off[2]);
+                tma_load_3d(a, &tA, kk - tap * ca.cin, m0 - b0 * ca.T + off, b0, &full[s]);
+            } else {
+                tma_load_2d(a, &tA, (kb0 + i) * BK, m0, &full[s]);
+            }
             tma_load_2d(a + L::A_BYTES, &tB, (kb0 + i) * BK, n0, &full[s]);
             issued = i + 1;
         }
@@ -252,7 +270,10 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
         const bool all_ok = __syncthreads_and(ok) != 0;
         if (tid == 0 && all_ok && nkb > 0) {
             const int cols = out_mode == OUT_F32 ? 32 : 64;   // columns per 128-byte block
-            for (int j = 0; j < BN / cols && n0 + j * cols < N; ++j) tma_store_2d(&tC, n0 + j * cols, m0, sm + j * (BM * 128));
+            for (int j = 0; j < BN / cols && n0 + j * cols < N; ++j) {
+                if (ca.T > 0) tma_store_3d(&tC, n0 + j * cols, ca.phase, m0, sm + j * (BM * 128));
+                else tma_store_2d(&tC, n0 + j * cols, m0, sm + j * (BM * 128));
+            }
             bulk_commit();
             bulk_wait_all();   // the stores have read the stage buffers and written the output
         }
@@ -344,16 +365,28 @@ int sm_count()
 }
 
 template <int BN, int ST>
-int launch(const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tc, int out_mode, int M, int N, int K,
-           int splits, int kper, const Epilogue &e, float *ws, int *err, cudaStream_t st)
+int launch(const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tc, int out_mode, const ConvA &ca, int M,
+           int N, int K, int splits, int kper, const Epilogue &e, float *ws, int *err, cudaStream_t st)
 {
     using L = GemmSmem<BN, ST>;
     static std::atomic<uint64_t> done{0};
     poe::smem_attr_once(k_gemm<BN, ST>, L::TOTAL, done);
     const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
-    k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, tc, out_mode, M, N, K, kper, e, splits > 1 ? ws : nullptr,
-                                               err);
+    k_gemm<BN, ST><<<grid, NT, L::TOTAL, st>>>(ta, tb, tc, out_mode, ca, M, N, K, kper, e,
+                                               splits > 1 ? ws : nullptr, err);
     return (int)cudaGetLastError();
+}
+
+// the tile kernel for BN columns and a stage count by the k-blocks per CTA
+int launch_any(int BN, bool short_k, const CUtensorMap &ta, const CUtensorMap &tb, const CUtensorMap &tc,
+               int out_mode, const ConvA &ca, int M, int N, int K, int splits, int kper, const Epilogue &e, float *ws,
+               int *err, cudaStream_t st)
+{
+    return BN == 128
+               ? (short_k ? launch<128, 2>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st)
+                          : launch<128, 4>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st))
+               : (short_k ? launch<64, 2>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st)
+                          : launch<64, 4>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st));
 }
 }  // namespace
 
@@ -393,17 +426,68 @@ int gemm(const Gemm &g, const Epilogue &e, float *ws, int64_t ws_floats, int *er
             make_out_map(&tc, base, f32, g.M, g.N, e.ldc))
             out_mode = f32 ? OUT_F32 : OUT_BF16;
     }
-    int rc = BN == 128
-                 ? (short_k ? launch<128, 2>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st)
-                            : launch<128, 4>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st))
-                 : (short_k ? launch<64, 2>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st)
-                            : launch<64, 4>(ta, tb, tc, out_mode, g.M, g.N, g.K, splits, kper, e, ws, err, st));
+    int rc = launch_any(BN, short_k, ta, tb, tc, out_mode, ConvA{}, g.M, g.N, g.K, splits, kper, e, ws, err, st);
     if (rc || splits == 1) return rc;
     const int64_t total = (int64_t)g.M * g.N;
     int blocks = (int)((total + 255) / 256);
     if (blocks > 4 * sm_count()) blocks = 4 * sm_count();
     k_splitk_reduce<<<blocks, 256, 0, st>>>(ws, splits, g.M, g.N, e);
     return (int)cudaGetLastError();
+}
+
+int gemm_conv1d(const __nv_bfloat16 *x, int B, int T, int cin, int up, int phase, const __nv_bfloat16 *W, int cout,
+                const Epilogue &e, int *err, cudaStream_t st)
+{
+    if (B <= 0 || T <= 0 || (T & (T - 1)) || cin <= 0 || cin % BK || cout <= 0 || (up != 1 && up != 2) ||
+        phase < 0 || phase >= up || e.accumulate || (e.out_f32 == nullptr) == (e.out_bf16 == nullptr) ||
+        e.ldc < cout || ((uintptr_t)x & 15) || ((uintptr_t)W & 15))
+        return (int)cudaErrorInvalidValue;
+    const bool f32 = e.out_f32 != nullptr;
+    void *out = f32 ? (void *)e.out_f32 : (void *)e.out_bf16;
+    const int es = f32 ? 4 : 2;
+    if ((e.ldc * es) % 16 || ((uintptr_t)out & 15)) return (int)cudaErrorInvalidValue;
+    EncodeFn fn = encode_fn();
+    if (!fn) return (int)cudaErrorInvalidValue;
+    const int K = 3 * cin, M = B * T, rows = T < BM ? T : BM;
+    // x as {cin, T, B}: a box of 64 channels x `rows` times x BM / rows items (128 rows in all)
+    CUtensorMap ta, tb, tc;
+    {
+        const cuuint64_t dims[3] = {(cuuint64_t)cin, (cuuint64_t)T, (cuuint64_t)B};
+        const cuuint64_t strides[2] = {(cuuint64_t)cin * 2, (cuuint64_t)T * cin * 2};
+        const cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)rows, (cuuint32_t)(BM / rows)};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        if (fn(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(x), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return (int)cudaErrorInvalidValue;
+    }
+    const int BN = cout > 64 ? 128 : 64;
+    if (!make_map(&tb, W, cout, K, K, BN)) return (int)cudaErrorInvalidValue;
+    // the output as {cout, up, M}: row up*r + phase of the upsampled time axis
+    {
+        const cuuint64_t dims[3] = {(cuuint64_t)cout, (cuuint64_t)up, (cuuint64_t)M};
+        const cuuint64_t strides[2] = {(cuuint64_t)e.ldc * es, (cuuint64_t)up * e.ldc * es};
+        const cuuint32_t box[3] = {(cuuint32_t)(128 / es), 1u, (cuuint32_t)BM};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        if (fn(&tc, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, out, dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return (int)cudaErrorInvalidValue;
+    }
+    // tap k of output time up*s + phase reads upsampled time up*s + phase + k - 1,
+    // which is x row floor((up*s + phase + k - 1) / up) = s + off[k]
+    ConvA ca;
+    ca.T = T;
+    ca.cin = cin;
+    ca.up = up;
+    ca.phase = phase;
+    for (int k = 0; k < 3; ++k) {
+        const int d = phase + k - 1;   // up*s + d
+        ca.off[k] = d >= 0 ? d / up : -1;
+    }
+    const int nkb = K / BK;
+    return launch_any(BN, nkb <= 4, ta, tb, tc, f32 ? OUT_F32 : OUT_BF16, ca, M, cout, K, 1, nkb, e, nullptr, err,
+                      st);
 }
 
 }  // namespace sg

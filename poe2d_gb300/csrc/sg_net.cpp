@@ -5,6 +5,8 @@
 //
 // Every layer is a GEMM over an im2col matrix (channels last):
 //   forward   out[M, Cout] = col[M, Kp] . W[Cout, Kp]^T + b  (ReLU)
+//             (the time convolutions read their input in place instead:
+//             sg::gemm_conv1d, one GEMM per phase of the upsampled axis)
 //   backward  dZ = dOut * (out > 0)
 //             dW[Cout, Kp] = dZ^T . col         (GEMM of dZ^T and col^T, K = M)
 //             db = column sums of dZ
@@ -197,10 +199,22 @@ int forward(poe_sg *net, const __nv_bfloat16 *maps, const float *scalars, int B,
         Layer &l = net->L[i];
         const int64_t M = (int64_t)B * l.rows_per_item;
         const __nv_bfloat16 *A = l.col;
+        if (l.kind == CONV1D) {
+            // the time convolutions read x in place, one GEMM per output phase of
+            // the upsampled axis (no im2col matrix; backward builds it)
+            sg::Epilogue e;
+            e.bias = net->w32 + l.b_off;
+            e.relu = l.relu;
+            e.ldc = l.cout;
+            if (i + 1 == net->L.size()) e.out_f32 = out;
+            else e.out_bf16 = l.out;
+            for (int p = 0; p < l.up; ++p)
+                SK(sg::gemm_conv1d(x, B, l.t, l.cin, l.up, p, net->w16 + l.w_off, l.cout, e, net->err, st));
+            x = l.out;
+            continue;
+        }
         if (l.kind == CONV2D) {
             SK(sg::im2col2d(x, B, l.h, l.w, l.cin, l.col, l.kp, st));
-        } else if (l.kind == CONV1D) {
-            SK(sg::im2col1d(x, B, l.t, l.cin, l.up, l.col, l.kp, st));
         } else if (i == 4) {   // first FC: flattened encoder output | scalars
             SK(sg::concat(x, 4096, scalars, POE_SG_SCALARS, B, net->cat, kCat, st));
             A = net->cat;
@@ -237,6 +251,8 @@ int backward(poe_sg *net, int B)
         }
         // bias gradient
         SK(sg::colsum(dz, M, l.cout, l.cout, net->g32 + l.b_off, net->colpart, st));
+        // a time convolution's im2col matrix (forward reads its input in place)
+        if (l.kind == CONV1D) SK(sg::im2col1d(net->L[i - 1].out, B, l.t, l.cin, l.up, l.col, l.kp, st));
         // weight gradient: dZ^T [cout x M] . A^T [kp x M]
         const __nv_bfloat16 *A = l.kind == FC ? (i == 4 ? net->cat : net->L[i - 1].out) : l.col;
         SK(sg::transpose(dz, M, l.cout, l.cout, net->s_dzt, M, st));

@@ -56,6 +56,24 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const void *desc, int c0,
         : "memory");
 }
 
+// 3-D tiled TMA load of box (c0 inner, c1, c2 outer); parts of the box
+// outside the tensor (c1 or c2 may be negative) arrive as zeros and count.
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *desc, int c0, int c1, int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(desc), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 3-D tiled TMA store (bulk async-group); c0, c1, c2 >= 0
+__device__ __forceinline__ void tma_store_3d(const void *desc, int c0, int c1, int c2, const void *src)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+                 ::"l"(desc), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+                 : "memory");
+}
+
 // 2-D tiled TMA store of box (c0 inner, c1 outer) from shared memory, in the
 // thread's bulk async-group; parts of the box outside the tensor are not
 // written.  c0 * element size must be a multiple of 16; c0, c1 >= 0.

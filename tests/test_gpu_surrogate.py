@@ -117,3 +117,19 @@ def test_adam_steps_match_numpy_adam(poe):
         assert np.array_equal(w16.view(np.uint32), R.bf16_bits(gw.astype(np.float32))), t
         w, m, v = gw, gm.astype(np.float64), gv.astype(np.float64)
     net.close()
+
+
+def test_forward_of_an_item_does_not_depend_on_its_batch(poe):
+    """Each gather depends on its own map only: the time convolutions read
+    whole items (several per 128-row tile at the short early lengths, with the
+    rows past an item's end as zeros), so a model's output is the same bits in
+    a batch of 1, 3 or 8."""
+    from poe2d_gb300.surrogate import Surrogate
+    net = Surrogate(max_batch=8, seed=5)
+    maps, sc, tgt = _batch(8, 2)
+    dm, ds, _ = _dev(maps, sc, tgt)
+    full = net.forward(dm, ds).cpu().numpy()
+    for n, first in ((1, 0), (3, 2), (1, 7)):
+        part = net.forward(dm[first:first + n].contiguous(), ds[first:first + n].contiguous()).cpu().numpy()
+        assert np.array_equal(part.view(np.uint32), full[first:first + n].view(np.uint32)), (n, first)
+    net.close()
