@@ -343,11 +343,13 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 // k + g / nitems.  Before the producer fills a buffer with a tile of step n it
 // waits until the tile's 3 x 3 neighbourhood (the cells its boxes read, and
 // the readers of the buffer it will overwrite) has completed step n-1, by
-// the shots' done flags; it publishes its own tiles' flags once the compute
-// warps have released their buffers.  A CTA only ever waits for items of
-// earlier steps, which every CTA finishes before it moves on, so the waits
-// cannot close a cycle; the producer keeps publishing its own finished items
-// while it waits.  Without MS (nk = 1) no tile waits for another.
+// the shots' done flags; a publisher warp publishes each of the CTA's tiles
+// once the compute warps have released its buffer, whatever the producer is
+// waiting for.  A producer only ever waits for items of earlier steps, which
+// were taken from the queue before its own and which their CTAs have already
+// handed to their compute warps (a CTA issues its items in the order it takes
+// them), so the waits cannot close a cycle: the first step of a launch waits
+// for none.  Without MS (nk = 1) no tile waits for another.
 template <int SM, bool KONE, bool MULTI, bool COEF, bool MS, int TZ>
 __global__ void __launch_bounds__(tile::Geo<TZ>::PNT + (MS ? 32 : 0), 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
