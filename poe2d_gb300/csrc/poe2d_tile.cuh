@@ -345,11 +345,11 @@ __device__ __forceinline__ bool compute_sync_and(bool v)
 // the readers of the buffer it will overwrite) has completed step n-1, by
 // the shots' done flags; a publisher warp publishes each of the CTA's tiles
 // once the compute warps have released its buffer, whatever the producer is
-// waiting for.  A producer only ever waits for items of earlier steps, which
-// were taken from the queue before its own and which their CTAs have already
-// handed to their compute warps (a CTA issues its items in the order it takes
-// them), so the waits cannot close a cycle: the first step of a launch waits
-// for none.  Without MS (nk = 1) no tile waits for another.
+// waiting for.  A producer only ever waits for items of the previous step,
+// which were taken from the queue before its own, and a CTA issues its items
+// in the order it takes them; the first step of a launch waits for none, so
+// by induction on the step every item is issued and finishes: the waits
+// cannot close a cycle.  Without MS (nk = 1) no tile waits for another.
 template <int SM, bool KONE, bool MULTI, bool COEF, bool MS, int TZ>
 __global__ void __launch_bounds__(tile::Geo<TZ>::PNT + (MS ? 32 : 0), 1)
 k_tile_pal(const ModelDev mp, const ModelDev *__restrict__ models, const StreamShot *__restrict__ shots,
