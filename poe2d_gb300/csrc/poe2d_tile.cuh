@@ -1059,7 +1059,11 @@ int tile_launch(const ModelDev &m, const ModelDev *models, const StreamShot *sho
     static std::atomic<uint64_t> done{0};
     auto kern = k_tile_pal<SM, KONE, MULTI, COEF, MS, TZ>;
     smem_attr_once(kern, (int)G::PAL_SMEM, done);
-    const int grid = nitems < sm_count() ? nitems : sm_count();   // persistent: one CTA per SM
+    // persistent: one CTA per SM, fewer if the launch has fewer items (a
+    // step-spanning launch counts every step's: CTAs past a step's tile count
+    // take the next step's tiles as their neighbourhoods finish)
+    const int64_t items_all = MS ? (int64_t)nk * nitems : nitems;
+    const int grid = items_all < sm_count() ? (int)items_all : sm_count();
     if (grid <= 0) return (int)cudaGetLastError();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
