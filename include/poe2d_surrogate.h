@@ -86,6 +86,13 @@ int poe_sg_gemm(const void *A, int32_t lda, const void *B, int32_t ldb, int32_t 
                 float alpha, const float *bias, int32_t relu, float *out_f32, void *out_bf16, int32_t ldc,
                 int32_t accumulate, float *ws, int64_t ws_floats, int32_t *err_dev, void *stream);
 
+/* Batch assembly for training: dst row r = src row idx[r] for r < n, rows of
+ * row_bytes bytes (a multiple of 4; src and dst 4-byte aligned); idx holds
+ * n int64 row indices, each below the caller's row count.  All pointers
+ * device pointers; runs on `stream`. */
+int poe_sg_gather_rows(const void *src, int64_t row_bytes, const int64_t *idx, int32_t n, void *dst,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

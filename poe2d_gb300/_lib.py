@@ -139,6 +139,7 @@ SYMBOLS = {
     "poe_sg_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float,
                                     C.POINTER(C.c_float)]),
     "poe_sg_launches": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "poe_sg_gather_rows": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "poe_sg_last_error": (C.c_char_p, [C.c_void_p]),
     "poe_sg_destroy": (None, [C.c_void_p]),
     "poe_ref_receivers": (C.c_int32, [C.POINTER(Grid), C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

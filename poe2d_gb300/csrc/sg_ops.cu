@@ -378,4 +378,45 @@ int concat(const __nv_bfloat16 *src, int ns, const float *extra, int ne, int B, 
     return (int)cudaGetLastError();
 }
 
+
+// dst row r = src row idx[r] (rows of vecs_per_row V's): one V per thread step
+template <class V>
+__global__ void k_gather_rows(const V *src, int64_t vecs_per_row, const int64_t *idx, int n, V *dst)
+{
+    const int64_t total = (int64_t)n * vecs_per_row;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / vecs_per_row, v = i - r * vecs_per_row;
+        dst[i] = src[idx[r] * vecs_per_row + v];
+    }
+}
+
+int gather_rows(const void *src, int64_t row_bytes, const int64_t *idx, int n, void *dst, cudaStream_t st)
+{
+    if (n < 0 || row_bytes <= 0 || row_bytes % 4 || ((uintptr_t)src & 3) || ((uintptr_t)dst & 3))
+        return (int)cudaErrorInvalidValue;
+    if (n == 0) return 0;
+    // 16-byte vectors where rows and bases allow, else 4-byte words
+    const bool v16 = row_bytes % 16 == 0 && ((uintptr_t)src & 15) == 0 && ((uintptr_t)dst & 15) == 0;
+    const int64_t vecs = row_bytes / (v16 ? 16 : 4), total = (int64_t)n * vecs;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 8 * 152) blocks = 8 * 152;
+    if (v16)
+        k_gather_rows<uint4><<<blocks, 256, 0, st>>>(static_cast<const uint4 *>(src), vecs, idx, n,
+                                                      static_cast<uint4 *>(dst));
+    else
+        k_gather_rows<uint32_t><<<blocks, 256, 0, st>>>(static_cast<const uint32_t *>(src), vecs, idx, n,
+                                                         static_cast<uint32_t *>(dst));
+    return (int)cudaGetLastError();
+}
+
 }  // namespace sg
+
+// ---- C ABI: the row gather on its own (device pointers; idx: n row indices
+// into src, each < the caller's row count)
+extern "C" int poe_sg_gather_rows(const void *src, int64_t row_bytes, const int64_t *idx, int32_t n, void *dst,
+                                  void *stream)
+{
+    if (!src || !dst || (n > 0 && !idx)) return 1;   // POE_EINVAL
+    const int rc = sg::gather_rows(src, row_bytes, idx, n, dst, (cudaStream_t)stream);
+    return rc == 0 ? 0 : (rc == (int)cudaErrorInvalidValue ? 1 : 5);
+}

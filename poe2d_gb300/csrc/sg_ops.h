@@ -30,5 +30,7 @@ int adam(float *w, const float *g, float *m, float *v, int64_t n, float lr_t, fl
 int to_bf16(const float *x, int64_t n, __nv_bfloat16 *y, cudaStream_t st);
 int concat(const __nv_bfloat16 *src, int ns, const float *extra, int ne, int B, __nv_bfloat16 *dst, int ldd,
            cudaStream_t st);
+// dst row r = src row idx[r] for r < n (rows of row_bytes, a multiple of 4)
+int gather_rows(const void *src, int64_t row_bytes, const int64_t *idx, int n, void *dst, cudaStream_t st);
 
 }  // namespace sg

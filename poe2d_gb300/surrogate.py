@@ -23,6 +23,22 @@ _LAYER_GEMMS = [(32 * 32, 18, 64), (16 * 16, 576, 128), (8 * 8, 1152, 128), (4 *
                 (256, 384, 64), (512, 192, 64), (1024, 192, 64), (1024, 192, 384)]
 
 
+def gather_rows(t, idx, stream=None):
+    """t[idx] for a contiguous CUDA tensor t and an int64 CUDA index vector,
+    by the library's row-gather kernel (poe_sg_gather_rows) on `stream`
+    (default: torch's current stream)."""
+    import torch
+    assert t.is_cuda and t.is_contiguous() and idx.dtype == torch.int64 and idx.is_cuda
+    out = torch.empty((idx.numel(),) + tuple(t.shape[1:]), dtype=t.dtype, device=t.device)
+    row = t[0].numel() * t.element_size() if t.shape[0] else 0
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = L.lib().poe_sg_gather_rows(C.c_void_p(t.data_ptr()), row, C.c_void_p(idx.data_ptr()), idx.numel(),
+                                    C.c_void_p(out.data_ptr()), C.c_void_p(st))
+    if rc != L.POE_OK:
+        raise PoeError(rc, "poe_sg_gather_rows")
+    return out
+
+
 def forward_flops_per_sample():
     """Multiply-add FLOPs (2 per MAC) of one gather's forward pass."""
     return sum(2 * m * k * n for m, k, n in _LAYER_GEMMS)

@@ -144,7 +144,7 @@ def main(argv=None):
     import torch
     import poe2d_gb300 as P
     from poe2d_gb300 import datagen as D
-    from poe2d_gb300.surrogate import Surrogate
+    from poe2d_gb300.surrogate import Surrogate, gather_rows
     P.lib()
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -189,8 +189,7 @@ def main(argv=None):
             for bi in range(nb):
                 idx = perm[bi * args.batch:(bi + 1) * args.batch]
                 lr = args.lr * 0.5 * (1.0 + math.cos(math.pi * it / steps))
-                tot += net.train_step(Mtr.index_select(0, idx), Str.index_select(0, idx), Ytr.index_select(0, idx),
-                                      lr)
+                tot += net.train_step(gather_rows(Mtr, idx), gather_rows(Str, idx), gather_rows(Ytr, idx), lr)
                 it += 1
             curve.append(tot / nb)
         torch.cuda.synchronize()

@@ -133,3 +133,17 @@ def test_forward_of_an_item_does_not_depend_on_its_batch(poe):
         part = net.forward(dm[first:first + n].contiguous(), ds[first:first + n].contiguous()).cpu().numpy()
         assert np.array_equal(part.view(np.uint32), full[first:first + n].view(np.uint32)), (n, first)
     net.close()
+
+
+@pytest.mark.parametrize("shape,dtype", [((40, 64, 64, 2), torch.bfloat16), ((40, 3), torch.float32),
+                                         ((40, 1024, 384), torch.bfloat16), ((5, 7), torch.int32)])
+def test_gather_rows_equals_indexing(poe, shape, dtype):
+    """The training batch gather (16-byte vectors, or 4-byte words for rows
+    such as the 3 scalars) returns t[idx] bit for bit, repeats included."""
+    from poe2d_gb300.surrogate import gather_rows
+    g = torch.Generator().manual_seed(len(shape) * 31 + shape[0])
+    t = (torch.randn(shape, generator=g) * 100).to(dtype).cuda()
+    idx = torch.randint(0, shape[0], (17,), generator=g).cuda()
+    got = gather_rows(t, idx)
+    torch.cuda.synchronize()
+    assert got.shape == (17,) + shape[1:] and torch.equal(got, t[idx])
