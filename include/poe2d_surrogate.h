@@ -50,7 +50,8 @@ int poe_sg_get_params(poe_sg *net, float *host, int64_t n);
 int poe_sg_set_params(poe_sg *net, const float *host, int64_t n);   /* resets Adam state */
 int poe_sg_get_grads(poe_sg *net, float *host, int64_t n);
 
-/* Inference: out [B, 1024, 384] FP32 (device). */
+/* Inference: out [B, 1024, 384] FP32 (device, 16-byte aligned; NULL: the
+ * network's own buffer). */
 int poe_sg_forward(poe_sg *net, const void *maps_bf16, const float *scalars, int32_t B, float *out);
 
 /* Forward, loss and backward: gradients stay in the network; *loss_out (host)

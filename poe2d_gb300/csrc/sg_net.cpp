@@ -477,6 +477,8 @@ int poe_sg_set_params(poe_sg *net, const float *host, int64_t n)
 int poe_sg_forward(poe_sg *net, const void *maps, const float *scalars, int32_t B, float *out)
 {
     if (!net || !maps || !scalars || B < 1 || B > net->bmax) return net ? fail(net, 1, "batch") : 1;
+    if (((uintptr_t)out & 15) != 0)   // the output layer writes it with TMA stores
+        return fail(net, 1, "out must be 16-byte aligned");
     int rc = forward(net, static_cast<const __nv_bfloat16 *>(maps), scalars, B, out ? out : net->out);
     if (rc) return rc;
     return check_err(net);

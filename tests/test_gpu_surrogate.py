@@ -147,3 +147,18 @@ def test_gather_rows_equals_indexing(poe, shape, dtype):
     got = gather_rows(t, idx)
     torch.cuda.synchronize()
     assert got.shape == (17,) + shape[1:] and torch.equal(got, t[idx])
+
+
+def test_forward_rejects_an_unaligned_output(poe):
+    """The output layer writes `out` with TMA stores: a pointer off a 16-byte
+    boundary is refused with POE_EINVAL, nothing is launched."""
+    from poe2d_gb300 import _lib as L
+    from poe2d_gb300.surrogate import Surrogate
+    net = Surrogate(max_batch=8, seed=1)
+    maps, sc, tgt = _batch(2, 3)
+    dm, ds, _ = _dev(maps, sc, tgt)
+    buf = torch.empty(2 * 1024 * 384 + 4, dtype=torch.float32, device="cuda")
+    rc = L.lib().poe_sg_forward(net.h, dm.data_ptr(), ds.data_ptr(), 2, buf.data_ptr() + 4)
+    assert rc == L.POE_EINVAL
+    net.forward(dm, ds, out=buf[4:].view(2, 1024, 384))      # 16 bytes in: accepted
+    net.close()
