@@ -162,6 +162,11 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
     // 16-byte vector stores where the row pitch keeps 16-column chunks aligned
     const bool vec32 = (e.ldc % 4) == 0 && (((uintptr_t)(partial ? (void *)partial : (void *)e.out_f32)) & 15) == 0;
     const bool vec16 = (e.ldc % 8) == 0 && (((uintptr_t)e.out_bf16) & 15) == 0;
+    // a staged output goes out block by block as soon as every warp has put its
+    // rows of the block in (the stores overlap the remaining TMEM reads); every
+    // thread's waits are over, so whether any gave up is known now
+    const bool staged = out_mode != OUT_THREADS;
+    const bool store_ok = staged ? __syncthreads_and(ok) != 0 : false;
 #pragma unroll 1
     for (int c2 = 0; c2 < BN / 32; ++c2) {
         // two 16-column TMEM loads in flight per wait
@@ -169,7 +174,7 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c2 * 32), vv[0]);
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c2 * 32 + 16), vv[1]);
         tmem_ld_wait();
-        if (!row_ok || !ok) continue;
+        if (row_ok && ok) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const uint32_t (&v)[16] = vv[h];
@@ -262,22 +267,22 @@ k_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorM
                 }
             }
         }
-    }
-    if (out_mode != OUT_THREADS) {
-        // the staged tile, once every thread's part is in: TMA stores of its
-        // 128-byte column blocks (rows and columns past M, N are not written)
-        fence_proxy_async_smem();
-        const bool all_ok = __syncthreads_and(ok) != 0;
-        if (tid == 0 && all_ok && nkb > 0) {
-            const int cols = out_mode == OUT_F32 ? 32 : 64;   // columns per 128-byte block
-            for (int j = 0; j < BN / cols && n0 + j * cols < N; ++j) {
+        }
+        // the 128-byte block this chunk completes: a 32-column block (FP32) after
+        // every chunk, a 64-column block (bf16) after every second one
+        if (staged && (out_mode == OUT_F32 || (c2 & 1))) {
+            fence_proxy_async_smem();
+            __syncthreads();
+            const int cols = out_mode == OUT_F32 ? 32 : 64, j = out_mode == OUT_F32 ? c2 : c2 >> 1;
+            if (tid == 0 && store_ok && nkb > 0 && n0 + j * cols < N) {
                 if (ca.T > 0) tma_store_3d(&tC, n0 + j * cols, ca.phase, m0, sm + j * (BM * 128));
                 else tma_store_2d(&tC, n0 + j * cols, m0, sm + j * (BM * 128));
+                bulk_commit();
             }
-            bulk_commit();
-            bulk_wait_all();   // the stores have read the stage buffers and written the output
         }
     }
+    if (staged && tid == 0 && store_ok && nkb > 0)
+        bulk_wait_read_all();   // the stores have read the stage buffers (the writes complete on their own)
     tc_fence_before();
     __syncthreads();
     if (warp == 2) tmem_dealloc(tmem, L::TMEM_COLS);

@@ -86,6 +86,9 @@ __device__ __forceinline__ void tma_store_2d(const void *desc, int c0, int c1, c
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // every bulk store of this thread's groups has completed (its writes performed)
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// every bulk store of this thread's groups has read its shared-memory source
+// (the source may be reused or released; the global writes complete on their own)
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 // this thread's shared-memory writes, before later async-proxy (TMA) reads of them
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
