@@ -4,7 +4,7 @@
 //
 // A and B are bf16, row-major with K contiguous (K-major), FP32 accumulation
 // in tensor memory.  One CTA of 128 threads computes a 128 x BN tile:
-//   thread 0    TMA producer: a 4-stage ring of 128x64 (A) and BNx64 (B)
+//   thread 0    TMA producer: a 2- or 3-stage ring of 128x64 (A) and BNx64 (B)
 //               tiles, 128-byte swizzled, one mbarrier per stage;
 //   thread 32   MMA issuer: four tcgen05.mma (K = 16 each) per stage, then
 //               tcgen05.commit frees the stage; a last commit signals the end;
@@ -39,9 +39,9 @@ using namespace sm103;
 namespace {
 constexpr int BM = 128, BK = 64, NT = 128;
 
-// ST pipeline stages: 4 for long reductions; 2 when a CTA sees at most 4
-// k-blocks, which keeps shared memory small enough for 3-4 CTAs per SM so
-// one CTA's epilogue overlaps another's loads and MMAs
+// ST pipeline stages: 3 for long reductions (2 CTAs per SM); 2 when a CTA
+// sees at most 4 k-blocks, which keeps shared memory small enough for 3 CTAs
+// per SM, so one CTA's epilogue overlaps another's loads and MMAs
 template <int BN, int ST>
 struct GemmSmem {
     static constexpr int STAGES = ST;
@@ -389,9 +389,9 @@ int launch_any(int BN, bool short_k, const CUtensorMap &ta, const CUtensorMap &t
 {
     return BN == 128
                ? (short_k ? launch<128, 2>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st)
-                          : launch<128, 4>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st))
+                          : launch<128, 3>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st))
                : (short_k ? launch<64, 2>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st)
-                          : launch<64, 4>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st));
+                          : launch<64, 3>(ta, tb, tc, out_mode, ca, M, N, K, splits, kper, e, ws, err, st));
 }
 }  // namespace
 
